@@ -1,0 +1,76 @@
+"""ctypes binding of libgammcor_gpu.so (the C ABI declared in include/gammcor_gpu.h).
+
+The library is loaded from the package directory. There is no fallback: if the
+shared object is missing or does not load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libgammcor_gpu.so"
+
+GC_OK = 0
+STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "GC_ECUSOLVER",
+                5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED"}
+PREC = {"fp64": 0, "bf16x3": 1, "tf32x3": 2}
+ERPA = {"symm1": 0, "cholesky": 1}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+# name -> (restype, argtypes); the list mirrors include/gammcor_gpu.h
+SIGNATURES = {
+    "gc_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _vp]),
+    "gc_destroy": (C.c_int, [_vp]),
+    "gc_last_error": (C.c_char_p, [_vp]),
+    "gc_synchronize": (C.c_int, [_vp]),
+    "gc_kernel_launches": (C.c_longlong, [_vp]),
+    "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),
+    "gc_prepare_nums": (C.c_int, [C.c_int, _dp, C.c_int, _ip, _ip]),
+    "gc_pair_space": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_double, _ip, _ip]),
+    "gc_tran4_gen": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp,
+                               _vp, _vp, C.c_int]),
+    "gc_tran4_factored": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int,
+                                    _vp, C.c_int, _vp, _vp, C.c_int]),
+    "gc_ab_cas_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp,
+                                 _vp, C.c_double, _vp, _vp, _dp]),
+    "gc_erpa": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int]),
+    "gc_ace_ne_erpa_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
+                                      _vp, C.c_int, _dp]),
+    "gc_acecorr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp, _vp,
+                             C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
+}
+
+_lib = None
+
+
+class GcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def load(path: Path | None = None):
+    """Load the library (once) and declare every entry point's prototype."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with gammcor_gb300.build.build()")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(ctx, code: int):
+    if code != GC_OK:
+        msg = load().gc_last_error(ctx).decode() if ctx else ""
+        raise GcError(code, msg)

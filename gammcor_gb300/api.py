@@ -1,0 +1,222 @@
+"""Host-side mirror of the reference routines on the AC-CAS (FOFO) path.
+
+Each function keeps the name and argument meaning of the GAMMCOR subroutine it
+replaces and calls the CUDA library through its C ABI. Device memory is held
+in torch tensors (plumbing only; no torch op computes anything on the path).
+Matrices returned with Fortran meaning are column-major: ``A[i, j]`` is
+``A(i+1, j+1)`` of the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ERPA, PREC, check, load
+
+THR_SEL_ACT = 1e-8
+THR_QVIRT = 1e-7
+
+
+class Context:
+    """A library context bound to one device and one CUDA stream."""
+
+    def __init__(self, device: int = 0, stream: torch.cuda.Stream | None = None):
+        lib = load()
+        self.device = device
+        self.stream = stream
+        h = C.c_void_p()
+        if stream is None:
+            stream = torch.cuda.current_stream(device)
+        self.stream = stream
+        s = C.c_void_p(stream.cuda_stream)
+        check(None, lib.gc_create(C.byref(h), device, s))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load().gc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def launches(self) -> int:
+        return int(load().gc_kernel_launches(self.h))
+
+    def sync(self):
+        check(self.h, load().gc_synchronize(self.h))
+
+
+_default: dict[int, Context] = {}
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default:
+        _default[device] = Context(device)
+    return _default[device]
+
+
+def _ptr(t: torch.Tensor) -> C.c_void_p:
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ValueError("expected a contiguous tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fortran_cols(t: torch.Tensor) -> torch.Tensor:
+    """Device copy of a matrix laid out column-major (Fortran), as a (cols, rows) tensor."""
+    return t.t().contiguous()
+
+
+# --------------------------------------------------------------- host helpers
+def gauleg(x1: float, x2: float, n: int):
+    """GauLeg (misc.f:828-865)."""
+    x = np.zeros(n)
+    w = np.zeros(n)
+    check(None, load().gc_gauleg(x1, x2, _dptr(x), _dptr(w), n))
+    return x, w
+
+
+def prepare_nums(occ: np.ndarray, nele: int):
+    """prepare_nums (initia.f:2996-3035) -> (Num0, Num1)."""
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    a, b = C.c_int(), C.c_int()
+    check(None, load().gc_prepare_nums(occ.shape[0], _dptr(occ), nele, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def pair_space(occ: np.ndarray, nele: int, ifl_core: int = 1, thr_sel_act: float = THR_SEL_ACT,
+               thr_qvirt: float = THR_QVIRT) -> np.ndarray:
+    """Pair builder of ACCAS (accas.f:30-106). Returns IndN as (NDimX, 2), 1-based."""
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    n = occ.shape[0]
+    buf = np.zeros(max(1, n * (n - 1)), dtype=np.int32)
+    nd = C.c_int()
+    check(None, load().gc_pair_space(n, _dptr(occ), nele, ifl_core, thr_sel_act, thr_qvirt,
+                                     _iptr(buf), C.byref(nd)))
+    return buf[: 2 * nd.value].reshape(-1, 2).astype(np.int64)
+
+
+# ----------------------------------------------------------------- transform
+def tran4_gen(nbas: int, CA: torch.Tensor, CB: torch.Tensor, CC: torch.Tensor, CD: torch.Tensor,
+              ao_sorted: torch.Tensor, precision: str = "fp64", ctx: Context | None = None,
+              out: torch.Tensor | None = None) -> torch.Tensor:
+    """tran4_gen (tran.f90:313-423).
+
+    CA..CD: AO x MO blocks as (nbas, nX) tensors with Fortran meaning (they are
+    made column-major here). ao_sorted: (ntr, ntr) AOTWOSORT records. Returns
+    the output file as (nA*nB, nC*nD): row = record ab, column = element cd.
+    """
+    ctx = ctx or default_context(CA.device.index or 0)
+    cols = [_fortran_cols(c.to(torch.float64)) for c in (CA, CB, CC, CD)]
+    nA, nB, nC, nD = (c.shape[0] for c in cols)
+    if out is None:
+        out = torch.empty((nA * nB, nC * nD), dtype=torch.float64, device=CA.device)
+    check(ctx.h, load().gc_tran4_gen(ctx.h, nbas, nA, _ptr(cols[0]), nB, _ptr(cols[1]), nC,
+                                     _ptr(cols[2]), nD, _ptr(cols[3]), _ptr(ao_sorted), _ptr(out),
+                                     PREC[precision]))
+    return out
+
+
+def tran4_factored(nbas: int, lfac: torch.Tensor, CA, CB, CC, CD, precision: str = "fp64",
+                   ctx: Context | None = None, out: torch.Tensor | None = None) -> torch.Tensor:
+    """tran4_gen's output from the ERI factor; lfac is (ntr, rank) with Fortran meaning."""
+    ctx = ctx or default_context(CA.device.index or 0)
+    cols = [_fortran_cols(c.to(torch.float64)) for c in (CA, CB, CC, CD)]
+    nA, nB, nC, nD = (c.shape[0] for c in cols)
+    lcol = _fortran_cols(lfac)
+    rank = lfac.shape[1]
+    if out is None:
+        out = torch.empty((nA * nB, nC * nD), dtype=torch.float64, device=CA.device)
+    same = CA is CC and CB is CD
+    cc = cols[0] if same else cols[2]
+    cd = cols[1] if same else cols[3]
+    check(ctx.h, load().gc_tran4_factored(ctx.h, nbas, rank, _ptr(lcol), nA, _ptr(cols[0]), nB,
+                                          _ptr(cols[1]), nC, _ptr(cc), nD, _ptr(cd), _ptr(out),
+                                          PREC[precision]))
+    return out
+
+
+# ------------------------------------------------------------------ assembly
+def ab_cas_fofo(occ: np.ndarray, xone: np.ndarray, indn: np.ndarray, nact: int, inactive: int,
+                ffoo: torch.Tensor, fofo: torch.Tensor, rdm2act: np.ndarray, acalpha: float,
+                ctx: Context | None = None):
+    """AB_CAS_FOFO (abfofo.f90:8-293). Returns (ABPLUS, ABMIN, ETot); the
+    matrices are (NDimX, NDimX) views with Fortran meaning (column-major storage)."""
+    ctx = ctx or default_context(ffoo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    xone = np.ascontiguousarray(xone, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    rdm = np.ascontiguousarray(rdm2act, dtype=np.float64)
+    n = occ.shape[0]
+    N = ind.shape[0] // 2
+    abp = torch.empty((N, N), dtype=torch.float64, device=ffoo.device)
+    abm = torch.empty_like(abp)
+    etot = C.c_double()
+    check(ctx.h, load().gc_ab_cas_fofo(ctx.h, n, inactive, nact, N, _dptr(occ), _dptr(xone),
+                                       _iptr(ind), _dptr(rdm), _ptr(ffoo), _ptr(fofo),
+                                       float(acalpha), _ptr(abp), _ptr(abm), C.byref(etot)))
+    return abp.t(), abm.t(), etot.value
+
+
+def erpasymm1(abplus: torch.Tensor, abmin: torch.Tensor, mode: str = "symm1",
+              ctx: Context | None = None):
+    """ERPASYMM1 (interpa.f:1652-1781) or its Cholesky form. abplus/abmin are
+    Fortran-meaning (N, N) matrices (column-major storage, e.g. the views
+    returned by ab_cas_fofo). Returns (EigVecR, Eig) with EigVecR[:, nu] = Y_nu."""
+    ctx = ctx or default_context(abplus.device.index or 0)
+    ap = abplus.t().contiguous()   # column-major storage
+    am = abmin.t().contiguous()
+    N = ap.shape[0]
+    y = torch.empty_like(ap)
+    eig = torch.empty(N, dtype=torch.float64, device=ap.device)
+    check(ctx.h, load().gc_erpa(ctx.h, N, _ptr(ap), _ptr(am), _ptr(y), _ptr(eig), ERPA[mode]))
+    return y.t(), eig
+
+
+def ace_ne_erpa_fofo(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray, indn: np.ndarray,
+                     nact: int, inactive: int, fofo: torch.Tensor, precision: str = "fp64",
+                     ctx: Context | None = None) -> float:
+    """ACEneERPA_FOFO (abfofo.f90:3791-3927): W(lambda)."""
+    ctx = ctx or default_context(fofo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    ycol = evec.t().contiguous()
+    w = C.c_double()
+    check(ctx.h, load().gc_ace_ne_erpa_fofo(ctx.h, occ.shape[0], inactive, nact, ind.shape[0] // 2,
+                                            _dptr(occ), _iptr(ind), _ptr(ycol),
+                                            _ptr(evals.contiguous()), _ptr(fofo), PREC[precision],
+                                            C.byref(w)))
+    return w.value
+
+
+def acecorr(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ngrid: int = 5,
+            erpa_mode: str = "symm1", precision: str = "fp64", ctx: Context | None = None):
+    """ACECORR (acfd.f:117-209). Returns (E_CAS, ECorr, [W(lambda_i)])."""
+    ctx = ctx or default_context(ffoo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    xone = np.ascontiguousarray(xone, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    rdm = np.ascontiguousarray(rdm2act, dtype=np.float64)
+    ec, ecas = C.c_double(), C.c_double()
+    ws = np.zeros(ngrid)
+    check(ctx.h, load().gc_acecorr(ctx.h, occ.shape[0], inactive, nact, ind.shape[0] // 2,
+                                   _dptr(occ), _dptr(xone), _iptr(ind), _dptr(rdm), _ptr(ffoo),
+                                   _ptr(fofo), ngrid, ERPA[erpa_mode], PREC[precision],
+                                   C.byref(ec), C.byref(ecas), _dptr(ws)))
+    return ecas.value, ec.value, list(ws)

@@ -1,0 +1,589 @@
+// ERPA A+B / A-B assembly in gather form.
+//
+// AB_CAS_FOFO (abfofo.f90:8-293) streams FOFO and FFOO records through
+// JK_loop (abfofo.f90:4468-5053) and scatters contributions into
+// ABPLUS(ipq,irs). Here every output element (ipq, irs) is computed by one
+// thread from closed forms of the same terms:
+//   * integral terms read FOFO / FFOO elements directly,
+//   * the 2-RDM terms T1..T6 read small intermediates Z (sums over two
+//     active indices of an integral times RDM2val) built once per system,
+//   * the one-body part reads HNO, AuxI, AuxIO and WMAT (n x n), which the
+//     reference accumulates in the same loops.
+// Every coefficient is 1, lambda or (1 - lambda), so A+-B is affine in lambda.
+#include "gc_internal.cuh"
+
+namespace {
+
+struct Geo {
+  int n, nin, nact, nocc;
+};
+
+__device__ __forceinline__ double Fofo(const double *__restrict__ f, const Geo &g, int a, int b,
+                                       int c, int d) {  // (ab|cd), b, d < nocc
+  size_t ld = (size_t)g.n * g.nocc;
+  return f[(size_t)(a + (size_t)b * g.n) * ld + c + (size_t)d * g.n];
+}
+__device__ __forceinline__ double Ffoo(const double *__restrict__ f, const Geo &g, int a, int b,
+                                       int c, int d) {  // (ab|cd), c, d < nocc
+  size_t ld = (size_t)g.n * g.n;
+  return f[(size_t)(c + (size_t)d * g.nocc) * ld + a + (size_t)b * g.n];
+}
+__device__ __forceinline__ double RV(const double *__restrict__ rv, int nocc, int i, int j, int k,
+                                     int l) {
+  return rv[i + (size_t)nocc * (j + (size_t)nocc * (k + (size_t)nocc * l))];
+}
+// AuxCoeff(g1,g2,g3,g4): 1 if the four orbital groups are equal, else lambda.
+__device__ __forceinline__ double AC(int a, int b, int c, int d, double lam) {
+  return (a == b && b == c && c == d) ? 1.0 : lam;
+}
+// AuxInd(g1,g2) of AB_CAS_FOFO: 1 for inactive/active combinations other than
+// active-active, 2 for active-active, 0 otherwise.
+__device__ __forceinline__ int AuxInd(int a, int b) {
+  if (a <= 1 && b <= 1) return (a == 1 && b == 1) ? 2 : 1;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// One-body matrices (lambda dependent): HNO, AuxI, AuxIO; column-major n x n.
+__global__ void k_onebody(Geo g, const double *__restrict__ h, const double *__restrict__ occ,
+                          const int *__restrict__ grp, const double *__restrict__ fofo,
+                          const double *__restrict__ ffoo, double lam, double *__restrict__ hno,
+                          double *__restrict__ auxi, double *__restrict__ auxio) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n || j >= g.n) return;
+  int gi = grp[i], gj = grp[j];
+  double hv = h[i + (size_t)j * g.n];
+  double corr = 0.0, ai = 0.0, aio = 0.0;
+  for (int k = 0; k < g.nocc; ++k) {
+    int gk = grp[k];
+    double ok = occ[k];
+    double jv = Ffoo(ffoo, g, i, j, k, k);          // (ij|kk)
+    double kv = Fofo(fofo, g, j, k, i, k);          // (jk|ik)
+    if (gi == gj && gk != gi) corr += ok * (2.0 * jv - kv);
+    double t = ok * (2.0 * AC(gi, gj, gk, gk, lam) * jv - AC(gi, gi, gj, gk, lam) * kv);
+    ai += t;
+    if (k < g.nin) aio += t;
+  }
+  size_t o = i + (size_t)j * g.n;
+  hno[o] = (gi != gj) ? lam * hv : hv + (1.0 - lam) * corr;
+  auxi[o] = ai;
+  auxio[o] = aio;
+}
+
+// WMAT(k, r) = sum_{l,i,j < nocc} AC(k,l,i,j) (kl|ij) RDM2val(i,j,r,l); zero for r >= nocc.
+__global__ void k_wmat(Geo g, const int *__restrict__ grp, const double *__restrict__ fofo,
+                       const double *__restrict__ rv, double lam, double *__restrict__ wmat) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  int r = blockIdx.y;
+  if (k >= g.n) return;
+  double s = 0.0;
+  if (r < g.nocc) {
+    int gk = grp[k];
+    for (int l = 0; l < g.nocc; ++l) {
+      int gl = grp[l];
+      for (int j = 0; j < g.nocc; ++j) {
+        int gj = grp[j];
+        for (int i = 0; i < g.nocc; ++i)
+          s += AC(gk, gl, grp[i], gj, lam) * Fofo(fofo, g, k, l, i, j) * RV(rv, g.nocc, i, j, r, l);
+      }
+    }
+  }
+  wmat[k + (size_t)r * g.n] = s;
+}
+
+// E_CAS two-electron part: sum_{ijkl < nocc} RDM2val(i,j,k,l) (ij|kl); per-block partials.
+__global__ void k_etwo(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+                       double *__restrict__ part) {
+  __shared__ double red[256];
+  size_t total = (size_t)g.nocc * g.nocc * g.nocc * g.nocc;
+  double s = 0.0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int i = t % g.nocc;
+    size_t r = t / g.nocc;
+    int j = r % g.nocc;
+    r /= g.nocc;
+    int k = r % g.nocc;
+    int l = (int)(r / g.nocc);
+    s += rv[t] * Ffoo(ffoo, g, i, j, k, l);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// ---------------------------------------------------------------------------
+// 2-RDM intermediates (lambda independent). Capital letters are orbital
+// indices T = nin + t of active orbitals; small letters index the active block.
+
+// Z1[a,b,c,d] = sum_tu (ab|TU) RV[T,U,C,D]; a < n, b < nocc, c,d < nact.
+__global__ void k_z1(Geo g, const double *__restrict__ fofo, const double *__restrict__ rv,
+                     double *__restrict__ z) {
+  size_t total = (size_t)g.n * g.nocc * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int a = t % g.n;
+    size_t r = t / g.n;
+    int b = r % g.nocc;
+    r /= g.nocc;
+    int c = r % g.nact, d = (int)(r / g.nact);
+    double s = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt)
+        s += Fofo(fofo, g, a, b, g.nin + tt, g.nin + u) *
+             RV(rv, g.nocc, g.nin + tt, g.nin + u, g.nin + c, g.nin + d);
+    z[t] = s;
+  }
+}
+
+// Z4[r,p,q,s] = sum_tu (rU|pT) RV[T,Q,S,U];  Z7[r,p,q,s] = sum_tu (rU|pT) RV[T,Q,U,S].
+__global__ void k_z47(Geo g, const double *__restrict__ fofo, const double *__restrict__ rv,
+                      double *__restrict__ z4, double *__restrict__ z7) {
+  size_t total = (size_t)g.n * g.n * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int p = t % g.n;
+    size_t r0 = t / g.n;
+    int r = r0 % g.n;
+    r0 /= g.n;
+    int q = r0 % g.nact, s = (int)(r0 / g.nact);
+    int Q = g.nin + q, S = g.nin + s;
+    double a4 = 0.0, a7 = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt) {
+        double f = Fofo(fofo, g, r, g.nin + u, p, g.nin + tt);
+        a4 += f * RV(rv, g.nocc, g.nin + tt, Q, S, g.nin + u);
+        a7 += f * RV(rv, g.nocc, g.nin + tt, Q, g.nin + u, S);
+      }
+    size_t o = r + (size_t)g.n * (p + (size_t)g.n * (q + (size_t)g.nact * s));
+    z4[o] = a4;
+    z7[o] = a7;
+  }
+}
+
+// Z5[r,q,p,s] = sum_tu (rU|Tq) RV[T,P,S,U];  Z6[r,q,p,s] = sum_tu (rU|Tq) RV[T,P,U,S].
+__global__ void k_z56(Geo g, const double *__restrict__ fofo, const double *__restrict__ rv,
+                      double *__restrict__ z5, double *__restrict__ z6) {
+  size_t total = (size_t)g.n * g.nocc * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int r = t % g.n;
+    size_t r0 = t / g.n;
+    int q = r0 % g.nocc;
+    r0 /= g.nocc;
+    int p = r0 % g.nact, s = (int)(r0 / g.nact);
+    int P = g.nin + p, S = g.nin + s;
+    double a5 = 0.0, a6 = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt) {
+        double f = Fofo(fofo, g, r, g.nin + u, g.nin + tt, q);
+        a5 += f * RV(rv, g.nocc, g.nin + tt, P, S, g.nin + u);
+        a6 += f * RV(rv, g.nocc, g.nin + tt, P, g.nin + u, S);
+      }
+    z5[t] = a5;
+    z6[t] = a6;
+  }
+}
+
+// Z8[q,s,p,r] = sum_tu (TU|qs) RV[T,U,P,R];  q,s < nocc.
+__global__ void k_z8(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+                     double *__restrict__ z) {
+  size_t total = (size_t)g.nocc * g.nocc * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int q = t % g.nocc;
+    size_t r0 = t / g.nocc;
+    int s = r0 % g.nocc;
+    r0 /= g.nocc;
+    int p = r0 % g.nact, r = (int)(r0 / g.nact);
+    double a = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt)
+        a += Ffoo(ffoo, g, g.nin + tt, g.nin + u, q, s) *
+             RV(rv, g.nocc, g.nin + tt, g.nin + u, g.nin + p, g.nin + r);
+    z[t] = a;
+  }
+}
+
+// Z9[p,r,q,s] = sum_kl (pr|KL) RV[Q,S,K,L].
+__global__ void k_z9(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+                     double *__restrict__ z) {
+  size_t total = (size_t)g.n * g.n * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int p = t % g.n;
+    size_t r0 = t / g.n;
+    int r = r0 % g.n;
+    r0 /= g.n;
+    int q = r0 % g.nact, s = (int)(r0 / g.nact);
+    double a = 0.0;
+    for (int l = 0; l < g.nact; ++l)
+      for (int k = 0; k < g.nact; ++k)
+        a += Ffoo(ffoo, g, p, r, g.nin + k, g.nin + l) *
+             RV(rv, g.nocc, g.nin + q, g.nin + s, g.nin + k, g.nin + l);
+    z[t] = a;
+  }
+}
+
+// Z10[q,s,p,r] = sum_tu (Tq|sU) RV[T,P,R,U];  Z13[q,s,p,r] = sum_tu (Tq|sU) RV[T,P,U,R].
+__global__ void k_z1013(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+                        double *__restrict__ z10, double *__restrict__ z13) {
+  size_t total = (size_t)g.nocc * g.nocc * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int q = t % g.nocc;
+    size_t r0 = t / g.nocc;
+    int s = r0 % g.nocc;
+    r0 /= g.nocc;
+    int p = r0 % g.nact, r = (int)(r0 / g.nact);
+    int P = g.nin + p, R = g.nin + r;
+    double a10 = 0.0, a13 = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt) {
+        double f = Ffoo(ffoo, g, g.nin + tt, q, s, g.nin + u);
+        a10 += f * RV(rv, g.nocc, g.nin + tt, P, R, g.nin + u);
+        a13 += f * RV(rv, g.nocc, g.nin + tt, P, g.nin + u, R);
+      }
+    z10[t] = a10;
+    z13[t] = a13;
+  }
+}
+
+// Z11[p,s,q,r] = sum_tu (Tp|sU) RV[T,Q,R,U];  Z12[p,s,q,r] = sum_tu (Tp|sU) RV[T,Q,U,R].
+__global__ void k_z1112(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+                        double *__restrict__ z11, double *__restrict__ z12) {
+  size_t total = (size_t)g.n * g.nocc * g.nact * g.nact;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int p = t % g.n;
+    size_t r0 = t / g.n;
+    int s = r0 % g.nocc;
+    r0 /= g.nocc;
+    int q = r0 % g.nact, r = (int)(r0 / g.nact);
+    int Q = g.nin + q, R = g.nin + r;
+    double a11 = 0.0, a12 = 0.0;
+    for (int u = 0; u < g.nact; ++u)
+      for (int tt = 0; tt < g.nact; ++tt) {
+        double f = Ffoo(ffoo, g, g.nin + tt, p, s, g.nin + u);
+        a11 += f * RV(rv, g.nocc, g.nin + tt, Q, R, g.nin + u);
+        a12 += f * RV(rv, g.nocc, g.nin + tt, Q, g.nin + u, R);
+      }
+    z11[t] = a11;
+    z12[t] = a12;
+  }
+}
+
+struct Zs {
+  const double *z1, *z4, *z7, *z5, *z6, *z8, *z9, *z10, *z13, *z11, *z12;
+};
+
+// ---------------------------------------------------------------------------
+// A+B and A-B, element (row = pair i, column = pair j), column-major N x N.
+__global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__restrict__ pq,
+                     const double *__restrict__ occ, const int *__restrict__ grp,
+                     const double *__restrict__ fofo, const double *__restrict__ ffoo, Zs Z,
+                     const double *__restrict__ hno, const double *__restrict__ auxi,
+                     const double *__restrict__ auxio, const double *__restrict__ wmat, double lam,
+                     double *__restrict__ abp, double *__restrict__ abm) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= N) return;
+  const int n = g.n, nin = g.nin, nocc = g.nocc, na = g.nact;
+  int p = pp[i], q = pq[i], r = pp[j], s = pq[j];
+  int gp = grp[p], gq = grp[q], gr = grp[r], gs = grp[s];
+  double op = occ[p], oq = occ[q], orr = occ[r], os = occ[s];
+  double vp = 0.0, vm = 0.0, v;
+  double ac = AC(gp, gq, gr, gs, lam);
+  auto ai = [](int a, int b) { return AuxInd(a, b) == 1; };
+  double X1 = (ai(gp, gr) ? op * orr : 0.0) + (ai(gq, gs) ? oq * os : 0.0) -
+              (ai(gq, gr) ? oq * orr : 0.0) - (ai(gp, gs) ? op * os : 0.0);
+  if (r >= nin && p >= nin) {
+    // FOFO Coulomb: A- += 4 AC X1 (rs|pq) (its two A+ parts cancel)
+    vm += 4.0 * ac * X1 * Fofo(fofo, g, r, s, p, q);
+    // FOFO exchange: AC X1 (ps|rq)
+    v = ac * X1 * Fofo(fofo, g, p, s, r, q);
+    vp += v;
+    vm -= v;
+    // FFOO exchange: -AC X1 (pr|qs)
+    v = -ac * X1 * Ffoo(ffoo, g, p, r, q, s);
+    vp += v;
+    vm += v;
+  }
+  const bool pa = gp == 1, qa = gq == 1, ra = gr == 1, sa = gs == 1;
+  const int pA = p - nin, qA = q - nin, rA = r - nin, sA = s - nin;
+  // FOFO T1 (p -> q)
+  if (p >= nin && ra && qa) {
+    v = AC(gp, gs, 1, 1, lam) * Z.z1[p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA))];
+    vp += v;
+    vm -= v;
+  }
+  // FOFO T3
+  if (r >= nin && sa && pa) {
+    v = AC(gq, gr, 1, 1, lam) * Z.z1[r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA))];
+    vp += v;
+    vm -= v;
+  }
+  if (r >= nin && sa) {
+    if (qa && p >= nin) {
+      size_t o = r + (size_t)n * (p + (size_t)n * (qA + (size_t)na * sA));
+      double c = AC(gp, gr, 1, 1, lam);
+      v = c * Z.z4[o];  // T4
+      vp += v;
+      vm += v;
+      v = -c * Z.z7[o];  // T6 (p -> q)
+      vp += v;
+      vm -= v;
+    }
+    if (pa) {
+      size_t o = r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA));
+      double c = AC(gq, gr, 1, 1, lam);
+      v = c * Z.z5[o];  // T4 (p -> q)
+      vp += v;
+      vm -= v;
+      v = -c * Z.z6[o];  // T6
+      vp += v;
+      vm += v;
+    }
+  }
+  if (ra && pa) {
+    size_t o = q + (size_t)nocc * (s + (size_t)nocc * (pA + (size_t)na * rA));
+    double c = AC(gq, gs, 1, 1, lam);
+    v = c * Z.z8[o];  // FFOO T1
+    vp += v;
+    vm += v;
+    v = c * Z.z10[o];  // T2
+    vp += v;
+    vm += v;
+    v = -c * Z.z13[o];  // T5 (p -> q)
+    vp += v;
+    vm -= v;
+  }
+  if (sa && r >= nin && qa && p >= nin) {  // FFOO T3
+    v = AC(gp, gr, 1, 1, lam) * Z.z9[p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA))];
+    vp += v;
+    vm += v;
+  }
+  if (ra && qa && p >= nin) {
+    size_t o = p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA));
+    double c = AC(gp, gs, 1, 1, lam);
+    v = c * Z.z11[o];  // T2 (p -> q)
+    vp += v;
+    vm -= v;
+    v = -c * Z.z12[o];  // T5
+    vp += v;
+    vm += v;
+  }
+  // one-body part (final loop of AB_CAS_FOFO)
+  auto aux = [&](int ga, int gb, int x, int y) -> double {
+    int a = AuxInd(ga, gb);
+    if (a == 1) return auxi[x + (size_t)y * n];
+    if (a == 2) return auxio[x + (size_t)y * n];
+    return 0.0;
+  };
+  double v1 = 0.0;
+  if (p == r)
+    v1 += (op - os) * hno[q + (size_t)s * n] - wmat[q + (size_t)s * n] + op * aux(gp, gr, q, s);
+  if (q == s)
+    v1 += (oq - orr) * hno[p + (size_t)r * n] - wmat[p + (size_t)r * n] + oq * aux(gq, gs, p, r);
+  vp += v1;
+  vm += v1;
+  double v2 = 0.0;
+  if (q == r)
+    v2 += (oq - os) * hno[p + (size_t)s * n] - wmat[p + (size_t)s * n] + oq * aux(gq, gr, p, s);
+  if (p == s)
+    v2 += (op - orr) * hno[q + (size_t)r * n] - wmat[q + (size_t)r * n] + op * aux(gp, gs, q, r);
+  vp += v2;
+  vm -= v2;
+  double Cp = op >= 0.5 ? sqrt(op) : -sqrt(op), Cq = oq >= 0.5 ? sqrt(oq) : -sqrt(oq);
+  double Cr = orr >= 0.5 ? sqrt(orr) : -sqrt(orr), Cs = os >= 0.5 ? sqrt(os) : -sqrt(os);
+  double d = (Cp + Cq) * (Cr + Cs);
+  if (d != 0.0) vp /= d;
+  d = (Cp - Cq) * (Cr - Cs);
+  if (d != 0.0) vm /= d;
+  size_t o = i + (size_t)j * N;
+  abp[o] = vp;
+  abm[o] = vm;
+}
+
+}  // namespace
+
+namespace gc {
+
+int set_error(gc_context *ctx, int code, const char *fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return code;
+}
+
+int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int ndimx,
+               const double *occ, const double *xone, const int *indn, const double *rdm2act) {
+  if (nbas <= 0 || ninact < 0 || nact < 0 || ninact + nact > nbas || ndimx <= 0 || !occ ||
+      !indn || (!rdm2act && nact > 0))
+    return set_error(ctx, GC_EINVAL, "system: bad arguments nbas=%d ninact=%d nact=%d ndimx=%d",
+                     nbas, ninact, nact, ndimx);
+  const int n = nbas, nocc = ninact + nact;
+  sd.n = n;
+  sd.nin = ninact;
+  sd.nact = nact;
+  sd.nocc = nocc;
+  sd.ndimx = ndimx;
+  std::vector<int> grp(n), pp(ndimx), pq(ndimx);
+  for (int i = 0; i < n; ++i) grp[i] = i < ninact ? 0 : (i < nocc ? 1 : 2);
+  for (int i = 0; i < ndimx; ++i) {
+    int a = indn[2 * i] - 1, b = indn[2 * i + 1] - 1;
+    if (a < 0 || b < 0 || a >= n || b >= n || a <= b || b >= nocc)
+      return set_error(ctx, GC_EINVAL, "system: pair %d = (%d,%d) is not a p>q pair with q occupied",
+                       i + 1, a + 1, b + 1);
+    pp[i] = a;
+    pq[i] = b;
+  }
+  GC_TRY(sd.occ.upload(ctx, occ, n));
+  GC_TRY(sd.grp.upload(ctx, grp.data(), n));
+  GC_TRY(sd.pair_p.upload(ctx, pp.data(), ndimx));
+  GC_TRY(sd.pair_q.upload(ctx, pq.data(), ndimx));
+  if (xone) {
+    std::vector<double> h((size_t)n * n);
+    size_t t = 0;
+    for (int q = 0; q < n; ++q)
+      for (int p = 0; p <= q; ++p, ++t) {
+        h[p + (size_t)q * n] = xone[t];
+        h[q + (size_t)p * n] = xone[t];
+      }
+    GC_TRY(sd.h.upload(ctx, h.data(), h.size()));
+  }
+  // RDM2val(i,j,k,l) = FRDM2(i,k,j,l) (abfofo.f90:84-92, interpa.f:5244-5272)
+  std::vector<double> rv((size_t)nocc * nocc * nocc * nocc, 0.0);
+  auto frdm2 = [&](int ip, int iq, int ir, int is) -> double {
+    double r = 0.0;
+    if (ip == ir && iq == is && (occ[ip] == 1.0 || occ[iq] == 1.0)) r += 2.0 * occ[ip] * occ[iq];
+    if (ip == is && iq == ir && (occ[ip] == 1.0 || occ[iq] == 1.0)) r -= occ[ip] * occ[iq];
+    if (ip >= ninact && iq >= ninact && ir >= ninact && is >= ninact) {
+      long long i12 = (long long)(ip - ninact) * nact + (iq - ninact) + 1;
+      long long i34 = (long long)(ir - ninact) * nact + (is - ninact) + 1;
+      long long mx = i12 > i34 ? i12 : i34, mn = i12 > i34 ? i34 : i12;
+      r = rdm2act[mx * (mx - 1) / 2 + mn - 1];
+    }
+    return r;
+  };
+  for (int l = 0; l < nocc; ++l)
+    for (int k = 0; k < nocc; ++k)
+      for (int j = 0; j < nocc; ++j)
+        for (int i = 0; i < nocc; ++i)
+          rv[i + (size_t)nocc * (j + (size_t)nocc * (k + (size_t)nocc * l))] = frdm2(i, k, j, l);
+  GC_TRY(sd.rv.upload(ctx, rv.data(), rv.size()));
+  return GC_OK;
+}
+
+// Intermediates that depend only on the system, cached per assembly call set.
+struct ZBufs {
+  DevBuf<double> z1, z4, z7, z5, z6, z8, z9, z10, z13, z11, z12;
+};
+
+static int build_z(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
+                   ZBufs &Zb) {
+  Geo g{sd.n, sd.nin, sd.nact, sd.nocc};
+  size_t na2 = (size_t)sd.nact * sd.nact;
+  size_t s1 = (size_t)sd.n * sd.nocc * na2, s4 = (size_t)sd.n * sd.n * na2,
+         s8 = (size_t)sd.nocc * sd.nocc * na2;
+  size_t one = 1;
+  GC_TRY(Zb.z1.alloc(ctx, std::max(s1, one)));
+  GC_TRY(Zb.z4.alloc(ctx, std::max(s4, one)));
+  GC_TRY(Zb.z7.alloc(ctx, std::max(s4, one)));
+  GC_TRY(Zb.z5.alloc(ctx, std::max(s1, one)));
+  GC_TRY(Zb.z6.alloc(ctx, std::max(s1, one)));
+  GC_TRY(Zb.z8.alloc(ctx, std::max(s8, one)));
+  GC_TRY(Zb.z9.alloc(ctx, std::max(s4, one)));
+  GC_TRY(Zb.z10.alloc(ctx, std::max(s8, one)));
+  GC_TRY(Zb.z13.alloc(ctx, std::max(s8, one)));
+  GC_TRY(Zb.z11.alloc(ctx, std::max(s1, one)));
+  GC_TRY(Zb.z12.alloc(ctx, std::max(s1, one)));
+  if (sd.nact == 0) return GC_OK;
+  auto grid = [](size_t total) { return std::min<unsigned>(ceil_div(total, 256), 152u * 64u); };
+  k_z1<<<grid(s1), 256, 0, ctx->stream>>>(g, fofo, sd.rv.p, Zb.z1.p);
+  GC_LAUNCHED(ctx);
+  k_z47<<<grid(s4), 256, 0, ctx->stream>>>(g, fofo, sd.rv.p, Zb.z4.p, Zb.z7.p);
+  GC_LAUNCHED(ctx);
+  k_z56<<<grid(s1), 256, 0, ctx->stream>>>(g, fofo, sd.rv.p, Zb.z5.p, Zb.z6.p);
+  GC_LAUNCHED(ctx);
+  k_z8<<<grid(s8), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z8.p);
+  GC_LAUNCHED(ctx);
+  k_z9<<<grid(s4), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z9.p);
+  GC_LAUNCHED(ctx);
+  k_z1013<<<grid(s8), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z10.p, Zb.z13.p);
+  GC_LAUNCHED(ctx);
+  k_z1112<<<grid(s1), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z11.p, Zb.z12.p);
+  GC_LAUNCHED(ctx);
+  return GC_OK;
+}
+
+int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
+                double alpha, double *abplus, double *abmin, double *etot_host) {
+  Geo g{sd.n, sd.nin, sd.nact, sd.nocc};
+  const int n = sd.n, N = sd.ndimx;
+  ZBufs Zb;
+  GC_TRY(build_z(ctx, sd, ffoo, fofo, Zb));
+  DevBuf<double> hno, auxi, auxio, wmat;
+  GC_TRY(hno.alloc(ctx, (size_t)n * n));
+  GC_TRY(auxi.alloc(ctx, (size_t)n * n));
+  GC_TRY(auxio.alloc(ctx, (size_t)n * n));
+  GC_TRY(wmat.alloc(ctx, (size_t)n * n));
+  dim3 b2(16, 16), g2(ceil_div(n, 16), ceil_div(n, 16));
+  k_onebody<<<g2, b2, 0, ctx->stream>>>(g, sd.h.p, sd.occ.p, sd.grp.p, fofo, ffoo, alpha, hno.p,
+                                        auxi.p, auxio.p);
+  GC_LAUNCHED(ctx);
+  k_wmat<<<dim3(ceil_div(n, 128), n), 128, 0, ctx->stream>>>(g, sd.grp.p, fofo, sd.rv.p, alpha,
+                                                             wmat.p);
+  GC_LAUNCHED(ctx);
+  Zs Z{Zb.z1.p, Zb.z4.p, Zb.z7.p, Zb.z5.p, Zb.z6.p, Zb.z8.p, Zb.z9.p, Zb.z10.p, Zb.z13.p,
+       Zb.z11.p, Zb.z12.p};
+  dim3 b3(32, 8), g3(ceil_div(N, 32), ceil_div(N, 8));
+  k_ab<<<g3, b3, 0, ctx->stream>>>(g, N, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, ffoo,
+                                   Z, hno.p, auxi.p, auxio.p, wmat.p, alpha, abplus, abmin);
+  GC_LAUNCHED(ctx);
+  if (etot_host) {
+    const int nb = 120;
+    DevBuf<double> part;
+    GC_TRY(part.alloc(ctx, nb));
+    k_etwo<<<nb, 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, part.p);
+    GC_LAUNCHED(ctx);
+    double hpart[nb];
+    std::vector<double> occ(n), h((size_t)n * n);
+    GC_CUDA(ctx, cudaMemcpyAsync(hpart, part.p, sizeof hpart, cudaMemcpyDeviceToHost, ctx->stream));
+    GC_CUDA(ctx, cudaMemcpyAsync(occ.data(), sd.occ.p, n * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GC_CUDA(ctx, cudaMemcpyAsync(h.data(), sd.h.p, h.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double e1 = 0.0, e2 = 0.0;
+    for (int i = 0; i < sd.nocc; ++i) e1 += occ[i] * h[i + (size_t)i * n];
+    for (int b = 0; b < nb; ++b) e2 += hpart[b];
+    *etot_host = 2.0 * e1 + e2;
+  }
+  return GC_OK;
+}
+
+}  // namespace gc
+
+extern "C" int gc_ab_cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                              const double *occ, const double *xone, const int *indn,
+                              const double *rdm2act, const double *ffoo, const double *fofo,
+                              double alpha, double *abplus, double *abmin, double *etot) {
+  if (!ctx) return GC_EINVAL;
+  if (!xone || !ffoo || !fofo || !abplus || !abmin)
+    return gc::set_error(ctx, GC_EINVAL, "ab_cas_fofo: null pointer");
+  gc::SysDev sd;
+  GC_TRY(gc::sys_upload(ctx, sd, nbas, ninact, nact, ndimx, occ, xone, indn, rdm2act));
+  GC_TRY(gc::assemble_ab(ctx, sd, ffoo, fofo, alpha, abplus, abmin, etot));
+  return GC_OK;
+}

@@ -1,0 +1,140 @@
+// Internal declarations shared by the translation units of libgammcor_gpu.
+#pragma once
+
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/gammcor_gpu.h"
+
+struct gc_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cublasHandle_t cublas = nullptr;
+  cusolverDnHandle_t cusolver = nullptr;
+  int *dev_info = nullptr;           // cuSOLVER info slot
+  int *dev_flag = nullptr;           // device error flag for bounded waits
+  long long launches = 0;            // kernels of this library launched
+  std::string err;
+};
+
+namespace gc {
+
+// Status propagation --------------------------------------------------------
+int set_error(gc_context *ctx, int code, const char *fmt, ...);
+
+#define GC_CUDA(ctx, call)                                                        \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return gc::set_error((ctx), GC_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__,  \
+                           #call, cudaGetErrorString(e_));                        \
+  } while (0)
+
+#define GC_CUBLAS(ctx, call)                                                      \
+  do {                                                                            \
+    cublasStatus_t s_ = (call);                                                   \
+    if (s_ != CUBLAS_STATUS_SUCCESS)                                              \
+      return gc::set_error((ctx), GC_ECUBLAS, "%s:%d %s: status %d", __FILE__,   \
+                           __LINE__, #call, (int)s_);                             \
+  } while (0)
+
+#define GC_CUSOLVER(ctx, call)                                                    \
+  do {                                                                            \
+    cusolverStatus_t s_ = (call);                                                 \
+    if (s_ != CUSOLVER_STATUS_SUCCESS)                                            \
+      return gc::set_error((ctx), GC_ECUSOLVER, "%s:%d %s: status %d", __FILE__, \
+                           __LINE__, #call, (int)s_);                             \
+  } while (0)
+
+#define GC_TRY(call)                 \
+  do {                               \
+    int r_ = (call);                 \
+    if (r_ != GC_OK) return r_;      \
+  } while (0)
+
+#define GC_LAUNCHED(ctx)                                                           \
+  do {                                                                             \
+    (ctx)->launches++;                                                             \
+    cudaError_t e_ = cudaGetLastError();                                           \
+    if (e_ != cudaSuccess)                                                         \
+      return gc::set_error((ctx), GC_ECUDA, "%s:%d launch: %s", __FILE__, __LINE__, \
+                           cudaGetErrorString(e_));                                \
+  } while (0)
+
+// Stream-ordered device buffer owned by a context call.
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    n = 0;
+  }
+  int alloc(gc_context *ctx, size_t count) {
+    release();
+    s = ctx->stream;
+    n = count;
+    if (count == 0) return GC_OK;
+    cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), ctx->stream);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return set_error(ctx, GC_ENOMEM, "cudaMallocAsync(%zu bytes): %s", count * sizeof(T),
+                       cudaGetErrorString(e));
+    }
+    return GC_OK;
+  }
+  int upload(gc_context *ctx, const T *host, size_t count) {
+    GC_TRY(alloc(ctx, count));
+    if (count)
+      GC_CUDA(ctx, cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return GC_OK;
+  }
+};
+
+inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// Per-system description resident on the device ------------------------------
+struct SysDev {
+  int n = 0, nin = 0, nact = 0, nocc = 0, ndimx = 0;
+  DevBuf<double> occ;      // (n)
+  DevBuf<int> grp;         // (n) 0 inactive, 1 active, 2 virtual
+  DevBuf<int> pair_p;      // (ndimx) 0-based p of pair (p > q)
+  DevBuf<int> pair_q;      // (ndimx)
+  DevBuf<double> h;        // (n, n) symmetrised one-electron MO matrix
+  DevBuf<double> rv;       // RDM2val (nocc^4), RV[i + nocc*(j + nocc*(k + nocc*l))]
+};
+
+// Host-side setup of SysDev (pairs, groups, RDM2val).
+int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int ndimx,
+               const double *occ, const double *xone, const int *indn, const double *rdm2act);
+
+// Assembly (gc_assembly.cu).
+int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
+                double alpha, double *abplus, double *abmin, double *etot_host);
+
+// ERPA (gc_erpa.cu).
+int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *eigvec,
+               double *eig, int mode);
+
+// Integrand (gc_integrand.cu).
+int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,
+              const double *fofo, int precision, double *w_host);
+
+// Elementwise helpers (gc_api.cu).
+int axpby_into(gc_context *ctx, size_t count, double a, const double *x, double b,
+               const double *y, double *out);
+
+}  // namespace gc

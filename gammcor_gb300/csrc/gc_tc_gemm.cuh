@@ -1,0 +1,22 @@
+// GEMM building blocks of the transform and the integrand, dispatched on
+// gc_precision: FP64 uses cuBLAS DGEMM; BF16X3 / TF32X3 run the split-precision
+// tcgen05 kernel of gc_tc_gemm.cu.
+#pragma once
+#include "gc_internal.cuh"
+
+namespace gc {
+
+// out_k (nX x nY, column-major, stride ostride) = CX^T M_k CY for cnt
+// column-major n x n matrices M_k; T1 is scratch of cnt*n*max(nX) doubles.
+int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M, int nX,
+                 const double *CX, int nY, const double *CY, double *T1, double *out,
+                 long long ostride);
+
+// C (m x n, column-major, ldc) = A (m x k, lda) . B (n x k, ldb)^T.
+int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double *A, int lda,
+               const double *B, int ldb, double *C, int ldc);
+
+int fp64_two_sided(gc_context *ctx, int n, int cnt, const double *M, int nX, const double *CX,
+                   int nY, const double *CY, double *T1, double *out, long long ostride);
+
+}  // namespace gc

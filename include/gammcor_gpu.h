@@ -1,0 +1,142 @@
+/*
+ * gammcor_gpu.h -- C ABI of the GB300 AC-CAS (FOFO) library.
+ *
+ * Conventions shared by every entry point
+ *  - Matrices are column-major with Fortran meaning: A(i,j) at A[i + j*ld].
+ *  - Orbital and pair indices passed in IndN are 1-based, as in the reference.
+ *  - "dev" arguments are device pointers on the context's device; "host"
+ *    arguments are host memory. Work is ordered on the context's stream.
+ *  - Every function returns a gc_status; GC_OK is 0. gc_last_error() gives a
+ *    one-line message for the last failure on a context.
+ *  - A context is not re-entrant: use one context per host thread.
+ */
+#ifndef GAMMCOR_GPU_H
+#define GAMMCOR_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gc_context gc_context;
+
+enum gc_status {
+  GC_OK = 0,
+  GC_EINVAL = 1,      /* bad argument */
+  GC_ECUDA = 2,       /* CUDA runtime error */
+  GC_ECUBLAS = 3,     /* cuBLAS error */
+  GC_ECUSOLVER = 4,   /* cuSOLVER error (eigensolver did not converge, ...) */
+  GC_ENOTPD = 5,      /* Cholesky found A+B not positive definite */
+  GC_ETIMEOUT = 6,    /* a bounded device wait ran out */
+  GC_ENOMEM = 7,      /* device allocation failed */
+  GC_EUNSUPPORTED = 8 /* shape or mode this build does not handle */
+};
+
+/* Arithmetic of the integral transform and of the integrand contraction. */
+enum gc_precision {
+  GC_PREC_FP64 = 0,    /* plain FP64 (cuBLAS DGEMM) */
+  GC_PREC_BF16X3 = 1,  /* split-BF16 3-pass on tcgen05 tensor cores, FP32 accumulate */
+  GC_PREC_TF32X3 = 2   /* split-TF32 3-pass on tcgen05 tensor cores, FP32 accumulate */
+};
+
+/* ERPA eigen-solver form. */
+enum gc_erpa_mode {
+  GC_ERPA_SYMM1 = 0,     /* ERPASYMM1: eig(A+), A+^1/2 A- A+^1/2, eig  (2 eigensolves) */
+  GC_ERPA_CHOLESKY = 1   /* A+ = L L^T, eig(L^T A- L), Y = L u / sqrt(2 w) (1 eigensolve) */
+};
+
+/* Context ------------------------------------------------------------- */
+/* cuda_stream is used as given; NULL selects the legacy default stream. */
+int gc_create(gc_context **ctx, int device, void *cuda_stream);
+int gc_destroy(gc_context *ctx);
+const char *gc_last_error(const gc_context *ctx);
+int gc_synchronize(gc_context *ctx);
+/* Number of kernels of this library launched on the context so far. */
+long long gc_kernel_launches(const gc_context *ctx);
+
+/* Host-side helpers ----------------------------------------------------- */
+
+/* GauLeg, misc.f:828-865: Gauss-Legendre abscissas x(n) and weights w(n) on [x1,x2]. */
+int gc_gauleg(double x1, double x2, double *x, double *w, int n);
+
+/* prepare_nums, initia.f:2996-3035: leading fully occupied (num0) and partially
+ * occupied (num1) orbital counts from Occ(nbas) and NELE. */
+int gc_prepare_nums(int nbas, const double *occ, int nele, int *num0, int *num1);
+
+/* Pair builder, accas.f:30-106 (IndN/IndX/NDimX of ACCAS). indn: host int
+ * array of capacity 2*nbas*(nbas-1)/2, filled as IndN(2,NDimX) 1-based. */
+int gc_pair_space(int nbas, const double *occ, int nele, int ifl_core,
+                  double thr_sel_act, double thr_qvirt, int *indn, int *ndimx);
+
+/* Integral transform -------------------------------------------------- */
+
+/* tran4_gen, tran.f90:313-423. ao_sorted_dev: the AOTWOSORT tensor as ntr
+ * records of ntr doubles (record rs holds (pq|rs) for packed pq, p<=q,
+ * pq = p + q(q-1)/2). CA..CD: AO x MO coefficient blocks (nbas x nX,
+ * column-major, device). out_dev: nA*nB records of nC*nD doubles, record
+ * ab = a + (b-1)*nA, element cd = c + (d-1)*nC (the FFOO/FOFO file layout). */
+int gc_tran4_gen(gc_context *ctx, int nbas,
+                 int nA, const double *CA_dev, int nB, const double *CB_dev,
+                 int nC, const double *CC_dev, int nD, const double *CD_dev,
+                 const double *ao_sorted_dev, double *out_dev, int precision);
+
+/* Same output as gc_tran4_gen from the ERI factor instead of the 4-index AO
+ * tensor: (pq|rs) = sum_P L(pq,P) L(rs,P), lfac_dev = L as (ntr x rank)
+ * column-major with the AOTWOSORT pair packing. No counterpart routine in the
+ * reference: it is the on-device AO ERI producer folded into tran4_gen. */
+int gc_tran4_factored(gc_context *ctx, int nbas, int rank, const double *lfac_dev,
+                      int nA, const double *CA_dev, int nB, const double *CB_dev,
+                      int nC, const double *CC_dev, int nD, const double *CD_dev,
+                      double *out_dev, int precision);
+
+/* A+B / A-B assembly ----------------------------------------------------- */
+
+/* AB_CAS_FOFO, abfofo.f90:8-293 with JK_loop, abfofo.f90:4468-5053
+ * (ICASSCF=1, AB1=.false., URe = identity as LdInteg leaves it).
+ *   occ_host(nbas), xone_host(nbas(nbas+1)/2) one-electron MO integrals,
+ *   indn_host IndN(2,ndimx) 1-based (IndX(i) = i), rdm2act_host active 2-RDM
+ *   in the NAddrRDM packing of rdm2.dat (value/2 as AB_CAS_FOFO stores it),
+ *   ffoo_dev/fofo_dev from gc_tran4_gen, alpha = ACAlpha.
+ * Writes abplus_dev/abmin_dev (ndimx x ndimx) and *etot_host (E_CAS w/o ENuc). */
+int gc_ab_cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                   const double *occ_host, const double *xone_host,
+                   const int *indn_host, const double *rdm2act_host,
+                   const double *ffoo_dev, const double *fofo_dev, double alpha,
+                   double *abplus_dev, double *abmin_dev, double *etot_host);
+
+/* ERPA ---------------------------------------------------------------------- */
+
+/* ERPASYMM1, interpa.f:1652-1781 (mode GC_ERPA_SYMM1), or the Cholesky form.
+ * abplus_dev/abmin_dev are read (and symmetrised in place). eigvec_dev(N,N)
+ * receives Y (column nu), eig_dev(N) omega (omega^2 where omega^2 <= 1e-6),
+ * ascending. */
+int gc_erpa(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
+            double *eigvec_dev, double *eig_dev, int mode);
+
+/* Integrand ---------------------------------------------------------------- */
+
+/* ACEneERPA_FOFO, abfofo.f90:3791-3927: *w_host = W(lambda) of the routine. */
+int gc_ace_ne_erpa_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                        const double *occ_host, const int *indn_host,
+                        const double *eigvec_dev, const double *eig_dev,
+                        const double *fofo_dev, int precision, double *w_host);
+
+/* Whole lambda quadrature ------------------------------------------------ */
+
+/* ACECORR, acfd.f:117-209 with ACEInteg_FOFO, abfofo.f90:3664-3789: for each
+ * Gauss-Legendre point lambda_i (ngrid points on [0,1]) assemble A+-B, solve
+ * ERPA and contract; *ecorr_host = sum_i w_i W(lambda_i), *ecas_host = E_CAS,
+ * w_out_host(ngrid) = W(lambda_i) (may be NULL).
+ * erpa_mode: GC_ERPA_SYMM1 reassembles A+-B at every point as the reference
+ * does; GC_ERPA_CHOLESKY assembles A+-B at lambda = 0 and 1 once and forms
+ * each point as A0 + lambda (A1 - A0). */
+int gc_acecorr(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+               const double *occ_host, const double *xone_host,
+               const int *indn_host, const double *rdm2act_host,
+               const double *ffoo_dev, const double *fofo_dev, int ngrid,
+               int erpa_mode, int precision,
+               double *ecorr_host, double *ecas_host, double *w_out_host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GAMMCOR_GPU_H */
