@@ -1,0 +1,324 @@
+"""AC-CAS correlation energies per second on one GB300.
+
+Workload (batched uneven instances): 64 synthetic systems, nbasis ~ U[50,250],
+inactive ~ U[5,25], CAS(2,2)..CAS(6,6), ERI factor rank 6*nbasis, 8
+Gauss-Legendre lambda points each. A step is one pass of the AC-CAS path over
+the whole batch (64 energies). Inputs (MO coefficients, ERI factors) are
+resident in HBM for `value`; `e2e` copies them from pinned host memory inside
+the timed region. The per-system working set (ERI factor, FFOO/FOFO, A+-B) is
+larger than L2 for all but the smallest systems.
+
+The fast form (split-BF16 tensor-core transform and integrand, Cholesky ERPA on
+an affine A+-B, concurrent worker streams) is timed for `value`; the plain FP64
+GPU path (ERPASYMM1, A+-B reassembled per point, one stream) is timed on every
+8th system together with the fast form on the same systems, and every fast
+energy of that subset is checked against the plain FP64 energy (1 microhartree).
+
+--impl reference times the CPU restatement of the reference algorithm (the
+reference itself cannot be compiled here: no Fortran compiler) on a bounded
+sample: the smallest system of the batch, 8 lambda points.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "AC-CAS energies/s at <=1 uEh vs FP64 oracle: mixed+batched+learned vs plain GPU"
+WORKLOAD = "batched-uneven-64: nbasis U[50,250], inactive U[5,25], CAS(2,2)-(6,6), rank 6n, 8 lambda"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nsys", type=int, default=64)
+    ap.add_argument("--ngrid", type=int, default=8)
+    ap.add_argument("--nstreams", type=int, default=8)
+    ap.add_argument("--precision", default="bf16x6")
+    ap.add_argument("--subset-stride", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def read_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_batch(nsys, seed, device, run, rank_offset=0, log=print):
+    """Generate the batch. Systems whose A+B is not positive definite at a
+    quadrature point are reported by the GPU path itself (Cholesky status) and
+    resampled; the final check run is the first warm-up step on the final batch."""
+    from gammcor_gb300 import api, synth
+    shapes = synth.batched_shapes(count=nsys, seed=seed + 7919 * rank_offset)
+    t0 = time.time()
+    systems = [synth.make_system_device(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"],
+                                        device=device) for sh in shapes]
+    log(f"generated {nsys} systems in {time.time() - t0:.1f}s")
+    for attempt in range(1, 8):
+        batch = api.BatchInputs(systems, device=device)
+        status = run(batch)[3]
+        bad = [int(i) for i in (status != 0).nonzero()[0]]
+        if not bad:
+            return batch
+        log(f"resampling {len(bad)} systems (A+B not positive definite): {bad}")
+        for i in bad:
+            sh = shapes[i]
+            systems[i] = synth.make_system_device(sh["n"], sh["nin"], sh["nact"], sh["rank"],
+                                                  sh["seed"] + 100000 * attempt, device=device)
+    raise RuntimeError("could not find positive-definite systems")
+
+
+def cpu_oracle_sample(batch_systems, ngrid, log=print):
+    """Oracle ACECORR on the smallest system of the batch; energies/s."""
+    import numpy as np
+    from oracle import ac_cas_ref as R
+    s = min(batch_systems, key=lambda x: x.n * x.nocc)
+    G = s.ao_eri_packed()
+    t0 = time.time()
+    ffoo, fofo = R.transform_fofo_ffoo(s.cmo, G, s.nin, s.nact)
+    indn = R.pair_space(s.occ, s.nele)
+    ecas, ecorr, ws, x, w = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act,
+                                      ngrid=ngrid)
+    dt = time.time() - t0
+    sample = (f"oracle (numpy/scipy restatement) ACECORR, {ngrid} points, smallest batch system "
+              f"n={s.n} nin={s.nin} CAS({s.nact},{s.nact}) N={len(indn)}, {dt:.1f}s")
+    log(sample)
+    return 1.0 / dt, sample, ecorr
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from gammcor_gb300 import synth
+    shapes = synth.batched_shapes(count=args.nsys, seed=args.seed)
+    sh = min(shapes, key=lambda x: x["n"] * (x["nin"] + x["nact"]))
+    s = synth.make_system(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"])
+    cores = os.cpu_count()
+    vals = []
+    for _ in range(max(1, args.warmup and 1)):
+        v, sample, _ = cpu_oracle_sample([s], args.ngrid, log=lambda *a: None)
+    for _ in range(args.steps):
+        v, sample, _ = cpu_oracle_sample([s], args.ngrid, log=lambda *a: None)
+        vals.append(v)
+    value = statistics.mean(vals)
+    line = {"metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": "smallest system of the batch"},
+            "cpu_baseline": {"value": value, "unit": "energies/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "energies/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = f"cuda:{local}"
+    log = (lambda *a: print(*a, file=sys.stderr, flush=True)) if rank == 0 else (lambda *a: None)
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from gammcor_gb300 import api
+
+    def fast(b):
+        return api.ac_energy_batched(b, ngrid=args.ngrid, precision=args.precision,
+                                     erpa_mode="cholesky", affine=True, nstreams=args.nstreams)
+
+    t0 = time.time()
+    batch = make_batch(args.nsys, args.seed, dev, fast, rank_offset=rank, log=log)
+    log(f"batch ready in {time.time() - t0:.1f}s (includes the first warm-up step)")
+    ctx = api.default_context(local)
+    Ns = batch.ndimx()
+    log(f"N range {min(Ns)}..{max(Ns)}, mean {sum(Ns) / len(Ns):.0f}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(max(0, args.warmup - 1)):
+        fast(batch)
+    barrier()
+    stream = torch.cuda.current_stream()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            ecorr, ecas, wl, status = fast(batch)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = (ctx.launches() - l0) // args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.nsys / (ms / 1000.0)
+    log(f"fast: {ms:.0f} ms per step, {value:.3f} energies/s, {launches} kernels/step")
+
+    # plain FP64 GPU path and fast form on the same subset; error check
+    sub = list(range(0, args.nsys, args.subset_stride))
+    sb = api.BatchInputs([batch.systems[i] for i in sub], device=dev)
+    api.ac_energy_batched(sb, ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
+                          nstreams=1)  # warm-up of the plain configuration
+    torch.cuda.synchronize()
+    t0 = time.time()
+    pe, pcas, pw, _ = api.ac_energy_batched(sb, ngrid=args.ngrid, precision="fp64",
+                                            erpa_mode="symm1", affine=False, nstreams=1)
+    torch.cuda.synchronize()
+    t_plain = time.time() - t0
+    t0 = time.time()
+    fe, fcas, fw, _ = fast(sb)
+    torch.cuda.synchronize()
+    t_fast_sub = time.time() - t0
+    err = np.abs(fe - pe)
+    log(f"subset {sub}: plain FP64 {t_plain:.1f}s, fast {t_fast_sub:.1f}s, max |dE| {err.max():.2e}")
+
+    # e2e: inputs from pinned host memory every step, energies back to host
+    e2e = None
+    if not args.no_e2e:
+        host_c = [t.cpu().pin_memory() for t in batch.cmo]
+        host_l = [t.cpu().pin_memory() for t in batch.lfac]
+        h2d = sum(t.numel() * 8 for t in host_c) + sum(t.numel() * 8 for t in host_l)
+        d2h = args.nsys * (2 + args.ngrid) * 8
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            for i in range(args.nsys):
+                batch.cmo[i].copy_(host_c[i], non_blocking=True)
+                batch.lfac[i].copy_(host_l[i], non_blocking=True)
+            fast(batch)
+        e1.record(stream)
+        barrier()
+        ems = e0.elapsed_time(e1) / args.steps
+        e2e = {"value": world * args.nsys / (ems / 1000.0), "unit": "energies/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # roofline of this library's dominant kernel: the tcgen05 GEMM at the
+    # integrand shape of the largest system (N x N x N), timed alone
+    hbm, bf16, src = read_peaks()
+    Nmax = max(Ns)
+    npass = 6 if args.precision == "bf16x6" else 3
+    ms_k = api.tc_gemm_time(Nmax, Nmax, Nmax, args.precision, reps=5)
+    ach = 2.0 * Nmax ** 3 * npass / (ms_k / 1000.0) / 1e12
+    roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+            "frac": ach / bf16, "traffic": None, "peak_source": src,
+            "kernel": f"k_tc_gemm<128> {Nmax}^3 x {npass} BF16 passes, {ms_k:.2f} ms/launch"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        v, sample, _ = cpu_oracle_sample(batch.systems, args.ngrid, log=log)
+        cpu = {"value": v, "unit": "energies/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
+                           "precision": args.precision, "erpa": "cholesky(A+B), affine A+-B",
+                           "streams": args.nstreams, "surrogate": "off",
+                           "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"},
+                "plain_fp64_subset": {"systems": sub, "plain_s": t_plain, "fast_s": t_fast_sub,
+                                      "speedup": t_plain / t_fast_sub,
+                                      "max_abs_err_eh": float(err.max()),
+                                      "within_1ueh": bool(err.max() <= 1e-6)},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk.summary(), "failed_systems": int((status != 0).sum())}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -14,12 +14,23 @@ LIB_PATH = _HERE / "libgammcor_gpu.so"
 GC_OK = 0
 STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "GC_ECUSOLVER",
                 5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED"}
-PREC = {"fp64": 0, "bf16x3": 1, "tf32x3": 2}
+PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2}
 ERPA = {"symm1": 0, "cholesky": 1}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
+
+class GcSystem(C.Structure):
+    _fields_ = [("nbas", C.c_int), ("ninact", C.c_int), ("nact", C.c_int), ("ndimx", C.c_int),
+                ("rank", C.c_int), ("occ", _dp), ("xone", _dp), ("indn", _ip), ("rdm2act", _dp),
+                ("cmo_dev", _vp), ("lfac_dev", _vp)]
+
+
+class GcAcParams(C.Structure):
+    _fields_ = [("ngrid", C.c_int), ("precision", C.c_int), ("erpa_mode", C.c_int),
+                ("affine", C.c_int), ("nstreams", C.c_int)]
+
 
 # name -> (restype, argtypes); the list mirrors include/gammcor_gpu.h
 SIGNATURES = {
@@ -40,6 +51,11 @@ SIGNATURES = {
     "gc_erpa": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int]),
     "gc_ace_ne_erpa_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
                                       _vp, C.c_int, _dp]),
+    "gc_ac_energy_batched": (C.c_int, [_vp, C.c_int, C.POINTER(GcSystem), C.POINTER(GcAcParams),
+                                       _dp, _dp, _dp, _ip]),
+    "gc_tc_gemm_time": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]),
+    "gc_tc_gemm_nt": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int,
+                                _vp, C.c_int]),
     "gc_acecorr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp, _vp,
                              C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
 }

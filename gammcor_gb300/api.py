@@ -220,3 +220,78 @@ def acecorr(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ngrid: int = 5
                                    _ptr(fofo), ngrid, ERPA[erpa_mode], PREC[precision],
                                    C.byref(ec), C.byref(ecas), _dptr(ws)))
     return ecas.value, ec.value, list(ws)
+
+
+def tc_gemm_nt(A: torch.Tensor, B: torch.Tensor, precision: str = "bf16x3",
+               ctx: Context | None = None) -> torch.Tensor:
+    """C = A @ B.T (FP64 in and out) through the tensor-core contraction engine."""
+    ctx = ctx or default_context(A.device.index or 0)
+    m, k = A.shape
+    n = B.shape[0]
+    acol = _fortran_cols(A)
+    bcol = _fortran_cols(B)
+    c = torch.empty((n, m), dtype=torch.float64, device=A.device)   # column-major m x n
+    check(ctx.h, load().gc_tc_gemm_nt(ctx.h, PREC[precision], m, n, k, _ptr(acol), m, _ptr(bcol),
+                                      n, _ptr(c), m))
+    return c.t()
+
+
+# ---------------------------------------------------------------------- batch
+class BatchInputs:
+    """Device-resident inputs of a batch of systems for ac_energy_batched."""
+
+    def __init__(self, systems, device="cuda:0"):
+        self.systems = list(systems)
+        self.device = device
+        self.cmo = [torch.as_tensor(np.asfortranarray(s.cmo).ravel(order="F"), device=device)
+                    for s in self.systems]
+        self.lfac = [torch.as_tensor(np.asfortranarray(s.lfac).ravel(order="F"), device=device)
+                     for s in self.systems]
+        self._host = []
+        self.indn = []
+        self.structs = (_lib.GcSystem * len(self.systems))()
+        for i, s in enumerate(self.systems):
+            indn = pair_space(s.occ, s.nele)
+            self.indn.append(indn)
+            occ = np.ascontiguousarray(s.occ, dtype=np.float64)
+            xone = np.ascontiguousarray(s.xone, dtype=np.float64)
+            ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+            rdm = np.ascontiguousarray(s.rdm2act, dtype=np.float64)
+            self._host.append((occ, xone, ind, rdm))
+            st = self.structs[i]
+            st.nbas, st.ninact, st.nact, st.ndimx, st.rank = s.n, s.nin, s.nact, len(indn), s.rank
+            st.occ, st.xone, st.indn, st.rdm2act = _dptr(occ), _dptr(xone), _iptr(ind), _dptr(rdm)
+        self.refresh_pointers()
+
+    def refresh_pointers(self):
+        for i in range(len(self.systems)):
+            self.structs[i].cmo_dev = self.cmo[i].data_ptr()
+            self.structs[i].lfac_dev = self.lfac[i].data_ptr()
+
+    def ndimx(self):
+        return [len(x) for x in self.indn]
+
+
+def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "bf16x6",
+                      erpa_mode: str = "cholesky", affine: bool = True, nstreams: int = 8,
+                      ctx: Context | None = None):
+    """ACECORR over a batch. Returns (ecorr, ecas, W[nsys, ngrid], status)."""
+    ctx = ctx or default_context(torch.device(batch.device).index or 0)
+    nsys = len(batch.systems)
+    par = _lib.GcAcParams(ngrid, PREC[precision], ERPA[erpa_mode], int(affine), nstreams)
+    ecorr = np.zeros(nsys)
+    ecas = np.zeros(nsys)
+    wl = np.zeros((nsys, ngrid))
+    status = np.zeros(nsys, dtype=np.int32)
+    check(ctx.h, load().gc_ac_energy_batched(ctx.h, nsys, batch.structs, C.byref(par),
+                                             _dptr(ecorr), _dptr(ecas), _dptr(wl), _iptr(status)))
+    return ecorr, ecas, wl, status
+
+
+def tc_gemm_time(m: int, n: int, k: int, precision: str = "bf16x6", reps: int = 10,
+                 ctx: Context | None = None) -> float:
+    """Milliseconds per launch of the tensor-core GEMM kernel (CUDA events)."""
+    ctx = ctx or default_context(0)
+    ms = C.c_double()
+    check(ctx.h, load().gc_tc_gemm_time(ctx.h, PREC[precision], m, n, k, reps, C.byref(ms)))
+    return ms.value

@@ -6,7 +6,9 @@
 //   Kt[pq, rs] = mask * (C_p+C_q)(C_r+C_s) (rs|pq)       (lambda independent)
 //   W = 2 sum_{i,nu} Yk[i,nu] (Kt Yk)[i,nu] - sum_pq mask (n_p(1-n_q)+n_q(1-n_p)) (pq|pq)
 // with Yk = Y restricted to 1e-3 < omega < 1e8. One GEMM and one reduction
-// replace N^2 dot products of length N.
+// replace N^2 dot products of length N. On the tensor-core path the diagonal of
+// Kt is taken out of the product and its term 2 Kt_ii (Yk Yk^T)_ii, which
+// nearly cancels the diagonal correction, is summed in FP64.
 #include "gc_internal.cuh"
 #include "gc_tc_gemm.cuh"
 
@@ -18,8 +20,8 @@ __device__ __forceinline__ double cicoef(double o) { return o >= 0.5 ? sqrt(o) :
 
 __global__ void k_kt(int n, int nocc, int N, const int *__restrict__ pp, const int *__restrict__ pq,
                      const double *__restrict__ occ, const int *__restrict__ grp,
-                     const double *__restrict__ fofo, double *__restrict__ kt,
-                     double *__restrict__ diag) {
+                     const double *__restrict__ fofo, int split_diag, double *__restrict__ kt,
+                     double *__restrict__ diag, double *__restrict__ kdiag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= N || j >= N) return;
@@ -28,11 +30,26 @@ __global__ void k_kt(int n, int nocc, int N, const int *__restrict__ pp, const i
   size_t ld = (size_t)n * nocc;
   double f = fofo[(size_t)(r + (size_t)s * n) * ld + p + (size_t)q * n];  // (rs|pq)
   double c = (cicoef(occ[p]) + cicoef(occ[q])) * (cicoef(occ[r]) + cicoef(occ[s]));
-  kt[i + (size_t)j * N] = same ? 0.0 : c * f;
+  double kv = same ? 0.0 : c * f;
+  kt[i + (size_t)j * N] = (split_diag && i == j) ? 0.0 : kv;
   if (i == j) {
     double op = occ[p], oq = occ[q];
     diag[i] = same ? 0.0 : -(op * (1.0 - oq) + oq * (1.0 - op)) * f;
+    kdiag[i] = kv;
   }
+}
+
+// diag[i] += 2 Kt_ii sum_nu Yk[i,nu]^2  (FP64)
+__global__ void k_diag_term(int N, const double *__restrict__ Yk, const double *__restrict__ kdiag,
+                            double *__restrict__ diag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s = 0.0;
+  for (int nu = 0; nu < N; ++nu) {
+    double y = Yk[i + (size_t)nu * N];
+    s += y * y;
+  }
+  diag[i] += 2.0 * kdiag[i] * s;
 }
 
 __global__ void k_mask_cols(int N, const double *__restrict__ Y, const double *__restrict__ eig,
@@ -74,32 +91,41 @@ int integrand(gc_context *ctx, const SysDev &sd, const double *Y, const double *
               const double *fofo, int precision, double *w_host) {
   const int N = sd.ndimx;
   const size_t NN = (size_t)N * N;
-  DevBuf<double> kt, yk, t, diag, part;
+  DevBuf<double> kt, yk, t, diag, kdiag, part;
   GC_TRY(kt.alloc(ctx, NN));
   GC_TRY(yk.alloc(ctx, NN));
-  GC_TRY(t.alloc(ctx, NN));
+  if (precision == GC_PREC_FP64) GC_TRY(t.alloc(ctx, NN));
   GC_TRY(diag.alloc(ctx, N));
+  GC_TRY(kdiag.alloc(ctx, N));
+  const int split = precision != GC_PREC_FP64;
   const int nb = 304;
   GC_TRY(part.alloc(ctx, nb));
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
   k_kt<<<g2, b2, 0, ctx->stream>>>(sd.n, sd.nocc, N, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p,
-                                   fofo, kt.p, diag.p);
+                                   fofo, split, kt.p, diag.p, kdiag.p);
   GC_LAUNCHED(ctx);
   k_mask_cols<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig, yk.p);
   GC_LAUNCHED(ctx);
-  // T = Kt Yk  ==  (Yk^T Kt^T)^T ; tc_gemm_nt computes C = A B^T with A = Kt, B = Yk^T.
   if (precision == GC_PREC_FP64) {
+    // T = Kt Yk, then W = 2 sum Yk .* T + sum diag
     const double one = 1.0, zero = 0.0;
     GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, &one, kt.p, N, yk.p,
                                N, &zero, t.p, N));
   } else {
-    // Kt is (N x N); B must be given as (n x k) = Yk^T, i.e. rows nu, columns i.
-    DevBuf<double> ykt;
-    GC_TRY(ykt.alloc(ctx, NN));
-    const double one = 1.0, zero = 0.0;
-    GC_CUBLAS(ctx, cublasDgeam(ctx->cublas, CUBLAS_OP_T, CUBLAS_OP_N, N, N, &one, yk.p, N, &zero,
-                               yk.p, N, ykt.p, N));
-    GC_TRY(tc_gemm_nt(ctx, precision, N, N, N, kt.p, N, ykt.p, N, t.p, N));
+    // off-diagonal Kt Yk on tensor cores with the dot product against Yk fused
+    // into the epilogue; the diagonal term in FP64
+    k_diag_term<<<ceil_div(N, 128), 128, 0, ctx->stream>>>(N, yk.p, kdiag.p, diag.p);
+    GC_LAUNCHED(ctx);
+    double dot = 0.0;
+    GC_TRY(tc_dot_gemm(ctx, precision, N, kt.p, yk.p, &dot));
+    std::vector<double> hd(N);
+    GC_CUDA(ctx, cudaMemcpyAsync(hd.data(), diag.p, N * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double dsum = 0.0;
+    for (double v : hd) dsum += v;
+    *w_host = 2.0 * dot + dsum;
+    return GC_OK;
   }
   k_contract<<<nb, 256, 0, ctx->stream>>>(NN, N, yk.p, t.p, diag.p, part.p);
   GC_LAUNCHED(ctx);

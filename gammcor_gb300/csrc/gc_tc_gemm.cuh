@@ -1,5 +1,5 @@
 // GEMM building blocks of the transform and the integrand, dispatched on
-// gc_precision: FP64 uses cuBLAS DGEMM; BF16X3 / TF32X3 run the split-precision
+// gc_precision: FP64 uses cuBLAS DGEMM; BF16X3 / BF16X6 run the split-precision
 // tcgen05 kernel of gc_tc_gemm.cu.
 #pragma once
 #include "gc_internal.cuh"
@@ -15,6 +15,11 @@ int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M
 // C (m x n, column-major, ldc) = A (m x k, lda) . B (n x k, ldb)^T.
 int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double *A, int lda,
                const double *B, int ldb, double *C, int ldc);
+
+// result = sum_{i,nu} (Ksym Y)[i,nu] * Y[i,nu] for a symmetric N x N Ksym and
+// an N x N Y (both column-major), with the product on tensor cores.
+int tc_dot_gemm(gc_context *ctx, int precision, int N, const double *Ksym, const double *Y,
+                double *result);
 
 int fp64_two_sided(gc_context *ctx, int n, int cnt, const double *M, int nX, const double *CX,
                    int nY, const double *CY, double *T1, double *out, long long ostride);

@@ -392,3 +392,120 @@ def batched_shapes(count: int = 64, seed: int = 2024):
         nact = int(rng.choice([2, 4, 6]))
         out.append(dict(n=n, nin=nin, nact=nact, rank=6 * n, seed=seed * 1000 + i))
     return out
+
+
+# ------------------------------------------------- device-side generation
+def make_system_device(n: int, nin: int, nact: int, rank: int, seed: int,
+                       eri_scale: float = ERI_SCALE, device: str = "cuda:0") -> System:
+    """make_system with the factor-based J/K builds, the SCF and the
+    canonicalisation run in FP64 torch on a GPU. The random draws are the
+    same numpy draws as make_system; results agree with it to rounding."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    lfac = make_lfac(n, rank, rng) * eri_scale
+    h = np.diag(rng.uniform(-20.0, 5.0, n))
+    off = rng.normal(0.0, 0.1, (n, n))
+    off = np.triu(off, 1)
+    h = h + off + off.T
+    q, r = np.linalg.qr(rng.standard_normal((n, n)))
+    guess = q * np.sign(np.diag(r))[None, :]
+    nele = nin + nact // 2
+    nocc = nin + nact
+
+    dev = torch.device(device)
+    p, qq = tri_index(n)
+    pt, qt = torch.as_tensor(p, device=dev), torch.as_tensor(qq, device=dev)
+    L = torch.as_tensor(lfac, device=dev)
+    Lsq = torch.zeros((rank, n, n), dtype=torch.float64, device=dev)
+    Lsq[:, pt, qt] = L.T
+    Lsq[:, qt, pt] = L.T
+    H = torch.as_tensor(h, device=dev)
+    eye = torch.eye(n, dtype=torch.float64, device=dev)
+
+    def jk(D, X):
+        Jv = torch.einsum('pmn,mn->p', Lsq, D)
+        J = torch.einsum('p,pmn->mn', Jv, Lsq)
+        Y = torch.matmul(Lsq, X)                      # (rank, n, k)
+        K = torch.einsum('pmi,pni->mn', Y, Y)
+        return J, K
+
+    # SCF (same scheme as scf())
+    c = torch.as_tensor(guess, device=dev)
+    D = c[:, :nele] @ c[:, :nele].T
+    fs, es = [], []
+    e_old = None
+    it = 0
+    for it in range(1, 61):
+        w, v = torch.linalg.eigh(D)
+        keep = w > 1e-12
+        X = v[:, keep] * torch.sqrt(w[keep])[None, :]
+        J, K = jk(D, X)
+        F = H + 2 * J - K
+        e = float(torch.sum(D * (H + F)))
+        err = F @ D - D @ F
+        emax = float(err.abs().max())
+        if e_old is not None and abs(e - e_old) < 1e-10 and emax < 1e-8:
+            break
+        e_old = e
+        if emax < 1e-2:
+            fs.append(F)
+            es.append(err)
+            fs, es = fs[-8:], es[-8:]
+            m = len(fs)
+            B = -torch.ones((m + 1, m + 1), dtype=torch.float64, device=dev)
+            B[m, m] = 0.0
+            for i in range(m):
+                for j in range(m):
+                    B[i, j] = torch.sum(es[i] * es[j])
+            rhs = torch.zeros(m + 1, dtype=torch.float64, device=dev)
+            rhs[m] = -1.0
+            try:
+                coef = torch.linalg.solve(B, rhs)[:m]
+                Fx = sum(ci * fi for ci, fi in zip(coef, fs))
+            except RuntimeError:
+                Fx = F
+            _, cc = torch.linalg.eigh(Fx)
+            D = cc[:, :nele] @ cc[:, :nele].T
+        else:
+            fs, es = [], []
+            _, cc = torch.linalg.eigh(F + 2.0 * (eye - D))
+            D = 0.5 * D + 0.5 * (cc[:, :nele] @ cc[:, :nele].T)
+    _, cmo_t = torch.linalg.eigh(F)
+
+    # frozen-core CAS-CI
+    ccore = cmo_t[:, :nin]
+    dcore = ccore @ ccore.T
+    Jc, Kc = jk(dcore, ccore)
+    fcore = H + 2 * Jc - Kc
+    e_core = float(torch.sum(dcore * (H + fcore)))
+    cact = cmo_t[:, nin:nocc]
+    h_eff = (cact.T @ fcore @ cact).cpu().numpy()
+    B = torch.matmul(torch.matmul(cact.T[None], Lsq), cact[None])        # (rank, nact, nact)
+    eri_act = torch.einsum('Pab,Pcd->abcd', B, B).cpu().numpy()
+    e_cas, g1, g2 = cas_ci(h_eff, eri_act, nact, e_core)
+
+    occ_act, u = np.linalg.eigh(0.5 * g1)
+    order = np.argsort(-occ_act, kind='stable')
+    occ_act, u = np.abs(occ_act[order]), u[:, order]
+    cmo = cmo_t.cpu().numpy().copy()
+    cmo[:, nin:nocc] = cmo[:, nin:nocc] @ u
+    g2no = np.einsum('pqrs,pa,qb,rc,sd->abcd', g2, u, u, u, u, optimize=True)
+    occ = np.zeros(n)
+    occ[:nin] = 1.0
+    occ[nin:nocc] = occ_act
+    cm = torch.as_tensor(cmo, device=dev)
+    Xo = cm[:, :nocc] * torch.sqrt(torch.as_tensor(occ[:nocc], device=dev))[None, :]
+    J, K = jk(Xo @ Xo.T, Xo)
+    fmo = (cm.T @ (H + 2 * J - K) @ cm).cpu().numpy()
+    if nin > 0:
+        _, ui = np.linalg.eigh(fmo[:nin, :nin])
+        cmo[:, :nin] = cmo[:, :nin] @ ui
+    if n > nocc:
+        _, uv = np.linalg.eigh(fmo[nocc:, nocc:])
+        cmo[:, nocc:] = cmo[:, nocc:] @ uv
+    xone = pack_sym(cmo.T @ h @ cmo)
+    del Lsq
+    return System(n=n, nin=nin, nact=nact, rank=rank, seed=seed, lfac=lfac, h_ao=h,
+                  cmo=cmo, occ=occ, xone=xone, rdm2act=pack_rdm2act(g2no),
+                  e_cas=e_cas, nele=nele, extra=dict(e_scf=e, scf_iter=it))

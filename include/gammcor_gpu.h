@@ -35,7 +35,8 @@ enum gc_status {
 enum gc_precision {
   GC_PREC_FP64 = 0,    /* plain FP64 (cuBLAS DGEMM) */
   GC_PREC_BF16X3 = 1,  /* split-BF16 3-pass on tcgen05 tensor cores, FP32 accumulate */
-  GC_PREC_TF32X3 = 2   /* split-TF32 3-pass on tcgen05 tensor cores, FP32 accumulate */
+  GC_PREC_BF16X6 = 2   /* three BF16 planes, 6 passes (products x_i y_j, i+j<=2): FP32-level
+                          product error, tcgen05 tensor cores, FP32 accumulate */
 };
 
 /* ERPA eigen-solver form. */
@@ -135,6 +136,55 @@ int gc_acecorr(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
                const double *ffoo_dev, const double *fofo_dev, int ngrid,
                int erpa_mode, int precision,
                double *ecorr_host, double *ecas_host, double *w_out_host);
+
+/* Batch of systems -------------------------------------------------------- */
+
+/* One AC-CAS instance: the arguments ACECORR receives (occupations, one-electron
+ * MO integrals, IndN, active 2-RDM) plus what LdInteg hands to tran4_gen (MO
+ * coefficients and the AO integrals, here as the ERI factor). */
+typedef struct gc_system {
+  int nbas, ninact, nact, ndimx, rank;
+  const double *occ;       /* host, nbas */
+  const double *xone;      /* host, nbas(nbas+1)/2 */
+  const int *indn;         /* host, IndN(2, ndimx), 1-based */
+  const double *rdm2act;   /* host, NAddrRDM-packed active 2-RDM */
+  const double *cmo_dev;   /* device, nbas x nbas AO x MO, column-major */
+  const double *lfac_dev;  /* device, ntr x rank ERI factor, column-major */
+} gc_system;
+
+typedef struct gc_ac_params {
+  int ngrid;       /* Gauss-Legendre points on [0,1] (5 in ACECORR) */
+  int precision;   /* gc_precision of the transform and the integrand */
+  int erpa_mode;   /* gc_erpa_mode */
+  int affine;      /* 1: assemble A+-B at lambda = 0 and 1 once, combine per point */
+  int nstreams;    /* concurrent worker streams */
+} gc_ac_params;
+
+/* ACECORR for nsys independent systems (no counterpart in the reference, which
+ * runs one system per process). ecorr/ecas (nsys), w_lambda (nsys*ngrid, may be
+ * NULL). status (nsys, may be NULL): per-system gc_status; when given, systems
+ * with A+B not positive definite (GC_ENOTPD) are reported there instead of
+ * failing the call. */
+int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *sys,
+                         const gc_ac_params *par, double *ecorr, double *ecas,
+                         double *w_lambda, int *status);
+
+/* Building block ---------------------------------------------------------- */
+
+/* C (m x n, ldc) = A (m x k, lda) . B (n x k, ldb)^T, all column-major FP64,
+ * computed in the given precision (GC_PREC_BF16X3 / GC_PREC_BF16X6 on the
+ * tcgen05 tensor cores, GC_PREC_FP64 with DGEMM). No counterpart routine in the
+ * reference: it is the contraction engine under tran4_gen and the integrand,
+ * exported so that it can be checked on its own. */
+int gc_tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k,
+                  const double *A_dev, int lda, const double *B_dev, int ldb,
+                  double *C_dev, int ldc);
+
+/* Average device time of one launch of the tensor-core GEMM kernel for an
+ * m x n x k product (operands prepared once, reps launches timed with CUDA
+ * events on the context stream). No counterpart in the reference. */
+int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int k, int reps,
+                    double *ms_per_launch);
 
 #ifdef __cplusplus
 }

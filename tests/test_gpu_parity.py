@@ -135,3 +135,28 @@ def test_acecorr_n64_golden():
         assert abs(ecas - float(d["ecas"])) < 1e-9
         assert abs(ecorr - float(d["ecorr"])) < 1e-9, (mode, ecorr, float(d["ecorr"]))
         np.testing.assert_allclose(ws, d["w_lambda"], atol=1e-9)
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 5e-5), ("bf16x6", 2e-7)])
+def test_tran4_mixed_precision_error(sys24, precision, tol):
+    """Mixed-precision transform vs the FP64 oracle: max |error| per integral."""
+    s, G, ffoo, fofo = sys24
+    gff, gfo = gpu_integrals(s, G, precision=precision)
+    err = max(np.abs(gff.cpu().numpy() - ffoo).max(), np.abs(gfo.cpu().numpy() - fofo).max())
+    assert err < tol, err
+    C = t(s.cmo)
+    co = C[:, :s.nocc].contiguous()
+    gfo2 = api.tran4_factored(s.n, t(s.lfac), C, co, C, co, precision=precision)
+    assert np.abs(gfo2.cpu().numpy() - fofo).max() < tol
+
+
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 1e-4), ("bf16x6", 5e-8)])
+def test_integrand_mixed_precision_error(sys24, precision, tol):
+    s, G, ffoo, fofo = sys24
+    indn = R.pair_space(s.occ, s.nele)
+    abp, abm, _ = R.ab_cas_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo,
+                                s.rdm2act, 0.5)
+    Y, eig, _ = R.erpasymm1(abp, abm)
+    w_ref = R.ac_ene_erpa_fofo(Y, eig, s.occ, s.nin, s.nact, indn, fofo)
+    w = api.ace_ne_erpa_fofo(t(Y), t(eig), s.occ, indn, s.nact, s.nin, t(fofo), precision=precision)
+    assert abs(w - w_ref) < tol, (w, w_ref)

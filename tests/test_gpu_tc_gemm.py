@@ -1,0 +1,36 @@
+"""The split-precision tcgen05 GEMM against an FP64 product.
+
+Error bounds, relative to the entries of |A| |B|^T: 3-pass BF16 (hi*hi +
+hi*lo + lo*hi) 2e-5; 6-pass BF16 (three planes) 1e-6 (FP32 accumulation
+dominates).
+"""
+import pytest
+import torch
+
+from gammcor_gb300 import api
+
+pytestmark = pytest.mark.gpu
+BOUND = {"bf16x3": 2e-5, "bf16x6": 1e-6}
+
+
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16x6"])
+@pytest.mark.parametrize("m,n,k", [(128, 128, 64), (200, 150, 300), (1000, 700, 513),
+                                   (7, 300, 40), (640, 90, 1500)])
+def test_tc_gemm_matches_fp64(gpu_lib, precision, m, n, k):
+    g = torch.Generator(device="cuda").manual_seed(m * 7 + n * 3 + k)
+    A = torch.randn(m, k, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(n, k, dtype=torch.float64, device="cuda", generator=g)
+    A[:, ::3] *= 1e-3          # mixed magnitudes
+    C = api.tc_gemm_nt(A, B, precision)
+    ref = A @ B.T
+    scale = (A.abs() @ B.abs().T)
+    err = ((C - ref).abs() / scale).max().item()
+    assert err < BOUND[precision], err
+
+
+def test_tc_gemm_repeated_calls_agree(gpu_lib):
+    A = torch.randn(300, 257, dtype=torch.float64, device="cuda")
+    B = torch.randn(190, 257, dtype=torch.float64, device="cuda")
+    c1 = api.tc_gemm_nt(A, B, "bf16x6")
+    c2 = api.tc_gemm_nt(A, B, "bf16x6")
+    assert torch.equal(c1, c2)
