@@ -56,6 +56,8 @@ SIGNATURES = {
     "gc_tc_gemm_time": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]),
     "gc_tc_gemm_nt": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int,
                                 _vp, C.c_int]),
+    "gc_ace_ne_erpa_fofo_noalloc": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip,
+                                              _vp, _vp, _vp, _dp]),
     "gc_acecorr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp, _vp,
                              C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
 }

@@ -205,6 +205,27 @@ def ace_ne_erpa_fofo(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray, i
     return w.value
 
 
+def ace_ne_erpa_fofo_noalloc(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray,
+                             indn: np.ndarray, nact: int, inactive: int, fofo: torch.Tensor,
+                             ctx: Context | None = None) -> float:
+    """W(lambda) through the entry point that allocates no device memory (for
+    callers that cannot allocate; limits nbas <= 2048, NDimX <= 16384). evec
+    must already be a Fortran-layout (column-major) device matrix, e.g. the
+    view returned by erpasymm1, so that no copy is made here."""
+    ctx = ctx or default_context(fofo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    ycol = evec.t()
+    if not ycol.is_contiguous():
+        raise ValueError("evec must be column-major (a .t() view of a contiguous tensor)")
+    w = C.c_double()
+    check(ctx.h, load().gc_ace_ne_erpa_fofo_noalloc(ctx.h, occ.shape[0], inactive, nact,
+                                                    ind.shape[0] // 2, _dptr(occ), _iptr(ind),
+                                                    _ptr(ycol), _ptr(evals), _ptr(fofo),
+                                                    C.byref(w)))
+    return w.value
+
+
 def acecorr(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ngrid: int = 5,
             erpa_mode: str = "symm1", precision: str = "fp64", ctx: Context | None = None):
     """ACECORR (acfd.f:117-209). Returns (E_CAS, ECorr, [W(lambda_i)])."""

@@ -121,6 +121,23 @@ int gc_ace_ne_erpa_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndi
                         const double *eigvec_dev, const double *eig_dev,
                         const double *fofo_dev, int precision, double *w_host);
 
+/* W(lambda) as gc_ace_ne_erpa_fofo computes it, for callers that cannot
+ * allocate device memory (a host whose device memory belongs to its own pool,
+ * code running during CUDA graph capture, a process that must not grow its
+ * device footprint). It allocates nothing: its working data lives in one fixed
+ * device array of this library (about 200 KB, held by every device that loads
+ * the library until the process exits), which limits it to nbas <= 2048 and
+ * ndimx <= 16384; larger sizes return GC_EINVAL. The first call on a device
+ * looks up that array's device address, so make it before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU (other streams,
+ * other contexts on the device) race. FP64 throughout; no counterpart routine
+ * in the reference. */
+int gc_ace_ne_erpa_fofo_noalloc(gc_context *ctx, int nbas, int ninact, int nact,
+                                int ndimx, const double *occ_host,
+                                const int *indn_host, const double *eigvec_dev,
+                                const double *eig_dev, const double *fofo_dev,
+                                double *w_host);
+
 /* Whole lambda quadrature ------------------------------------------------ */
 
 /* ACECORR, acfd.f:117-209 with ACEInteg_FOFO, abfofo.f90:3664-3789: for each
