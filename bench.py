@@ -8,8 +8,9 @@ resident in HBM for `value`; `e2e` copies them from pinned host memory inside
 the timed region. The per-system working set (ERI factor, FFOO/FOFO, A+-B) is
 larger than L2 for all but the smallest systems.
 
-The fast form (split-BF16 tensor-core transform and integrand, Cholesky ERPA on
-an affine A+-B, concurrent worker streams) is timed for `value`; the plain FP64
+The fast form (FP64-accurate sliced-BF16 tensor-core transform, ERPA products
+and integrand, Cholesky ERPA on an affine A+-B, concurrent worker streams) is
+timed for `value`; the plain FP64
 GPU path (ERPASYMM1, A+-B reassembled per point, one stream) is timed on every
 8th system together with the fast form on the same systems, and every fast
 energy of that subset is checked against the plain FP64 energy (1 microhartree).
@@ -45,7 +46,7 @@ def parse():
     ap.add_argument("--nsys", type=int, default=64)
     ap.add_argument("--ngrid", type=int, default=8)
     ap.add_argument("--nstreams", type=int, default=8)
-    ap.add_argument("--precision", default="bf16x6")
+    ap.add_argument("--precision", default="fp64tc5")
     ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-e2e", action="store_true")
@@ -283,12 +284,13 @@ def run_ours(args):
     # integrand shape of the largest system (N x N x N), timed alone
     hbm, bf16, src = read_peaks()
     Nmax = max(Ns)
-    npass = 6 if args.precision == "bf16x6" else 3
+    npass = {"bf16x3": 3, "bf16x6": 6, "fp64tc5": 15, "fp64tc6": 21}[args.precision]
     ms_k = api.tc_gemm_time(Nmax, Nmax, Nmax, args.precision, reps=5)
     ach = 2.0 * Nmax ** 3 * npass / (ms_k / 1000.0) / 1e12
     roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
             "frac": ach / bf16, "traffic": None, "peak_source": src,
-            "kernel": f"k_tc_gemm<128> {Nmax}^3 x {npass} BF16 passes, {ms_k:.2f} ms/launch"}
+            "kernel": f"tcgen05 GEMM ({args.precision}) {Nmax}^3 x {npass} BF16 passes, "
+                      f"{ms_k:.2f} ms/launch"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:

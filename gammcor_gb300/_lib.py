@@ -14,7 +14,7 @@ LIB_PATH = _HERE / "libgammcor_gpu.so"
 GC_OK = 0
 STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "GC_ECUSOLVER",
                 5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED"}
-PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2}
+PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "fp64tc5": 3, "fp64tc6": 4}
 ERPA = {"symm1": 0, "cholesky": 1}
 
 _dp = C.POINTER(C.c_double)

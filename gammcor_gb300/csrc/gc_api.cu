@@ -194,7 +194,7 @@ int gc_acecorr(gc_context *ctx, int nbas, int ninact, int nact, int ndimx, const
     } else {
       GC_TRY(gc::assemble_ab(ctx, sd, ffoo, fofo, lam, ap.p, am.p, ecas));
     }
-    GC_TRY(gc::erpa_solve(ctx, ndimx, ap.p, am.p, Y.p, eig.p, erpa_mode));
+    GC_TRY(gc::erpa_solve(ctx, ndimx, ap.p, am.p, Y.p, eig.p, erpa_mode, precision));
     double wi = 0.0;
     GC_TRY(gc::integrand(ctx, sd, Y.p, eig.p, fofo, precision, &wi));
     if (w_out) w_out[i] = wi;

@@ -64,7 +64,7 @@ int run_system(gc_context *ctx, const gc_system &s, const gc_ac_params &par, dou
     } else {
       GC_TRY(gc::assemble_ab(ctx, sd, ffoo.p, fofo.p, lam, ap.p, am.p, &e0));
     }
-    GC_TRY(gc::erpa_solve(ctx, N, ap.p, am.p, Y.p, eig.p, par.erpa_mode));
+    GC_TRY(gc::erpa_solve(ctx, N, ap.p, am.p, Y.p, eig.p, par.erpa_mode, par.precision));
     double wi = 0.0;
     GC_TRY(gc::integrand(ctx, sd, Y.p, eig.p, fofo.p, par.precision, &wi));
     if (w_out) w_out[i] = wi;

@@ -9,6 +9,7 @@
 // satisfies the same eigen-equation and normalisation, so W(lambda), which depends
 // on Y only through Y Y^T over kept modes, is unchanged. One eigensolve instead of two.
 #include "gc_internal.cuh"
+#include "gc_tc_gemm.cuh"
 
 namespace {
 
@@ -109,7 +110,7 @@ int syevd(gc_context *ctx, int N, double *A, double *w) {
 namespace gc {
 
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig,
-               int mode) {
+               int mode, int gemm_precision) {
   if (N <= 0 || !abplus || !abmin || !Y || !eig)
     return set_error(ctx, GC_EINVAL, "erpa: bad arguments N=%d", N);
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
@@ -173,15 +174,27 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     }
     k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
     GC_LAUNCHED(ctx);
-    // M = A- L (into Y as scratch), then M = L^T (A- L)
-    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N, Y, N));
-    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N, M.p, N));
-    GC_TRY(syevd(ctx, N, M.p, eig));
-    // Y = L U
-    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, M.p, N, Y, N));
+    const bool tc = gemm_precision == GC_PREC_FP64TC5 || gemm_precision == GC_PREC_FP64TC6;
+    if (tc) {
+      // T = A- L (into Y as scratch); M = L^T T; after the eigensolve Y = L U.
+      // Products of the FP64-accurate sliced tensor-core GEMM (L has a zero upper triangle).
+      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, abmin, 1, N, L.p, N, 1, Y, N));
+      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, N, 1, Y, N, 1, M.p, N));
+      k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
+      GC_LAUNCHED(ctx);
+      GC_TRY(syevd(ctx, N, M.p, eig));
+      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, 1, N, M.p, N, 1, Y, N));
+    } else {
+      // M = A- L (into Y as scratch), then M = L^T (A- L)
+      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N, Y, N));
+      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N, M.p, N));
+      GC_TRY(syevd(ctx, N, M.p, eig));
+      // Y = L U
+      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, M.p, N, Y, N));
+    }
     k_norm_chol<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig);
     GC_LAUNCHED(ctx);
     k_sqrt_eig<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(N, eig);
@@ -196,5 +209,5 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
 extern "C" int gc_erpa(gc_context *ctx, int ndimx, double *abplus, double *abmin, double *eigvec,
                        double *eig, int mode) {
   if (!ctx) return GC_EINVAL;
-  return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode);
+  return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, GC_PREC_FP64);
 }

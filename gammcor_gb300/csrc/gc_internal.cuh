@@ -126,8 +126,10 @@ int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const dou
                 double alpha, double *abplus, double *abmin, double *etot_host);
 
 // ERPA (gc_erpa.cu).
+// gemm_precision selects the arithmetic of the similarity and back-transform
+// products of the Cholesky form (GC_PREC_FP64 or a sliced FP64-accurate mode).
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *eigvec,
-               double *eig, int mode);
+               double *eig, int mode, int gemm_precision);
 
 // Integrand (gc_integrand.cu).
 int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,

@@ -282,6 +282,263 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
+// ------------------------------------------------ FP64-accurate (sliced) GEMM
+// Each row r of A is scaled by 2^-e_r (e_r: exponent of its largest entry) and
+// cut into S integer slices a = sum_t alpha_t 2^-7(t+1), |alpha_0| <= 128,
+// |alpha_t>0| <= 64, every alpha exact in BF16; likewise the rows of B with f_c.
+// C[r,c] = 2^(e_r+f_c) sum_{t+u<S} 2^-7(t+u+2) sum_k alpha_t[r,k] beta_u[c,k].
+// The products of one weight d = t+u share a TMEM accumulator; K is cut into
+// chunks short enough that every FP32 partial sum is an integer below 2^24, so
+// each chunk is exact, and the epilogue adds the chunks in FP64 registers.
+constexpr int OZ_BN = 64;
+constexpr int OZ_STAGES = 6;
+constexpr int OZ_MAXS = 6;
+
+struct OzPlan {
+  int S;          // slices per operand
+  int npass;      // S(S+1)/2
+  int chunk_kb;   // 64-wide K blocks per exact chunk
+  int pa[OZ_MAXS * (OZ_MAXS + 1) / 2], pb[OZ_MAXS * (OZ_MAXS + 1) / 2],
+      pd[OZ_MAXS * (OZ_MAXS + 1) / 2];
+};
+
+struct OzEpi {
+  int mode;              // 0 store, 1 dot with r
+  double *c;
+  long long ldn, sb;
+  const double *r;
+  double *partial;
+  const int *ea;         // row exponents of A, [batch][rows] (batch stride 0 if shared)
+  const int *eb;         // row exponents of B
+  long long ea_sb, eb_sb;
+};
+
+template <int S>
+__global__ void __launch_bounds__(192, 1)
+    k_tc_gemm_oz(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                 int M, int N, int kblocks, int a_batched, int b_batched, OzPlan plan, OzEpi epi,
+                 int *err_flag) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = OZ_BN * BK * 2;
+  uint8_t *sA = smem;
+  uint8_t *sB = smem + OZ_STAGES * A_BYTES;
+  uint64_t *full = (uint64_t *)(sB + OZ_STAGES * B_BYTES);
+  uint64_t *empty = full + OZ_STAGES;
+  uint64_t *accf = empty + OZ_STAGES;
+  uint64_t *acce = accf + 1;
+  uint32_t *tmem_slot = (uint32_t *)(acce + 1);
+  __shared__ int abort_flag;
+  __shared__ double red[4];
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * OZ_BN, b = blockIdx.z;
+  const int nchunks = (kblocks + plan.chunk_kb - 1) / plan.chunk_kb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < OZ_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accf, 1);
+    mbar_init(acce, 4);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(512u));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    int it = 0, issued = 0;
+    for (int g = 0; g < nchunks && !abort_flag; ++g) {
+      int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
+      for (int p = 0; p < plan.npass && !abort_flag; ++p)
+        for (int kb = kb0; kb < kb1; ++kb, ++it) {
+          int s = it % OZ_STAGES;
+          if (!mbar_wait(&empty[s], ((it / OZ_STAGES) & 1) ^ 1)) {
+            atomicExch(&abort_flag, 1);
+            break;
+          }
+          mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+          tma_load_4d(sA + s * A_BYTES, &mapA, &full[s], kb * BK, m0, a_batched ? b : 0, plan.pa[p]);
+          tma_load_4d(sB + s * B_BYTES, &mapB, &full[s], kb * BK, n0, b_batched ? b : 0, plan.pb[p]);
+          issued = it + 1;
+        }
+    }
+    if (abort_flag)
+      for (int j = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); j < issued; ++j)
+        mbar_wait(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1);
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = instr_desc(OZ_BN);
+    int it = 0;
+    bool ok = true;
+    for (int g = 0; g < nchunks && ok; ++g) {
+      if (g > 0 && !mbar_wait(acce, (g - 1) & 1)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
+      int last_d = -1;
+      for (int p = 0; p < plan.npass && ok; ++p) {
+        const int d = plan.pd[p];
+        const bool fresh = d != last_d;  // first pass of this weight in the chunk
+        last_d = d;
+        for (int kb = kb0; kb < kb1; ++kb, ++it) {
+          int s = it % OZ_STAGES;
+          if (!mbar_wait(&full[s], (it / OZ_STAGES) & 1) || abort_flag) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          uint32_t a_addr = smem_u32(sA + s * A_BYTES), b_addr = smem_u32(sB + s * B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk)
+            mma_bf16(tmem + (uint32_t)(d * OZ_BN), smem_desc(a_addr + kk * 32),
+                     smem_desc(b_addr + kk * 32), idesc, (fresh && kb == kb0 && kk == 0) ? 0u : 1u);
+          mma_commit(&empty[s]);
+        }
+      }
+      mma_commit(accf);
+    }
+    if (!ok) atomicExch(&abort_flag, 1);
+  } else if (warp >= 2) {
+    const int q = warp & 3;
+    const int m = m0 + q * 32 + lane;
+    double acc[OZ_BN];
+#pragma unroll
+    for (int j = 0; j < OZ_BN; ++j) acc[j] = 0.0;
+    bool ok = true;
+    for (int g = 0; g < nchunks && ok; ++g) {
+      if (!mbar_wait(accf, g & 1) || abort_flag) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int d = 0; d < S; ++d) {
+        const double w = ldexp(1.0, -7 * (d + 2));
+#pragma unroll
+        for (int c0 = 0; c0 < OZ_BN; c0 += 16) {
+          float v[16];
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * OZ_BN + c0), v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[c0 + j] += w * (double)v[j];
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(acce)) : "memory");
+    }
+    if (!ok) atomicExch(&abort_flag, 1);
+    double dot = 0.0;
+    if (ok && m < M) {
+      const int er = epi.ea[(long long)b * epi.ea_sb + m];
+#pragma unroll
+      for (int j = 0; j < OZ_BN; ++j) {
+        int n = n0 + j;
+        if (n < N) {
+          double cv = ldexp(acc[j], er + epi.eb[(long long)b * epi.eb_sb + n]);
+          long long o = (long long)b * epi.sb + m + (long long)n * epi.ldn;
+          if (epi.mode == 0)
+            epi.c[o] = cv;
+          else
+            dot += cv * epi.r[o];
+        }
+      }
+    }
+    if (epi.mode == 1) {
+      for (int off = 16; off > 0; off >>= 1) dot += __shfl_down_sync(0xffffffffu, dot, off);
+      if (lane == 0) red[warp - 2] = dot;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (epi.mode == 1 && threadIdx.x == 0) {
+    long long cta = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
+    epi.partial[cta] = red[0] + red[1] + red[2] + red[3];
+  }
+  if (threadIdx.x == 0 && abort_flag) atomicExch(err_flag, 1);
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512u));
+  }
+}
+
+// Row exponents: e[b][r] = 1 + ilogb(max_k |x[b,r,k]|) (0 for a zero row).
+__global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, int nb, long long sr,
+                               long long sk, long long sb, int *__restrict__ e) {
+  long long total = (long long)nb * rows;
+  // one warp per row
+  long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32;
+  int lane = threadIdx.x % 32;
+  for (long long t = wid; t < total; t += (long long)gridDim.x * blockDim.x / 32) {
+    int r = (int)(t % rows);
+    long long bb = t / rows;
+    const double *row = x + bb * sb + (long long)r * sr;
+    double mx = 0.0;
+    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(row[(long long)k * sk]));
+    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if (lane == 0) e[t] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+  }
+}
+
+// Integer slices: planes[t][b][r][kp] = alpha_t of x[b,r,k] 2^-e[b][r].
+__global__ void k_slice_planes(const double *__restrict__ x, int rows, int K, int Kp, int nb,
+                               long long sr, long long sk, long long sb, int S,
+                               const int *__restrict__ e, __nv_bfloat16 *__restrict__ planes) {
+  long long plane = (long long)nb * rows * Kp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < plane;
+       t += (long long)gridDim.x * blockDim.x) {
+    int k = (int)(t % Kp);
+    long long rr = t / Kp;
+    int r = (int)(rr % rows);
+    long long bb = rr / rows;
+    double v = k < K ? ldexp(x[bb * sb + (long long)r * sr + (long long)k * sk], -e[rr]) : 0.0;
+    for (int s = 0; s < S; ++s) {
+      v *= 128.0;
+      double a = rint(v);
+      v -= a;
+      planes[s * plane + t] = __double2bfloat16(a);
+    }
+  }
+}
+
+// Transposed-read variant (K is the slow index of x).
+__global__ void k_slice_planes_t(const double *__restrict__ x, int rows, int K, int Kp, int nb,
+                                 long long sr, long long sk, long long sb, int S,
+                                 const int *__restrict__ e, __nv_bfloat16 *__restrict__ planes) {
+  __shared__ double tile[32][33];
+  int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32, bb = blockIdx.z;
+  int tx = threadIdx.x, ty = threadIdx.y;
+  for (int i = ty; i < 32; i += 8) {
+    int k = k0 + i, r = r0 + tx;
+    tile[i][tx] = (k < K && r < rows) ? x[bb * sb + (long long)r * sr + (long long)k * sk] : 0.0;
+  }
+  __syncthreads();
+  long long plane = (long long)nb * rows * Kp;
+  for (int i = ty; i < 32; i += 8) {
+    int r = r0 + i, k = k0 + tx;
+    if (r >= rows || k >= Kp) continue;
+    double v = ldexp(tile[tx][i], -e[(long long)bb * rows + r]);
+    long long o = ((long long)bb * rows + r) * Kp + k;
+    for (int s = 0; s < S; ++s) {
+      v *= 128.0;
+      double a = rint(v);
+      v -= a;
+      planes[s * plane + o] = __double2bfloat16(a);
+    }
+  }
+}
+
 // ------------------------------------------------------------ operand packing
 // planes[s][b][r][kp] (bf16) from x[b*sb + r*sr + k*sk] (FP64): x = x0 + x1 + x2 + ...
 __global__ void k_pack_planes(const double *__restrict__ x, int rows, int K, int Kp, int nb,
@@ -440,6 +697,107 @@ int check_flag(gc_context *ctx) {
   return GC_OK;
 }
 
+
+// ---- sliced (FP64-accurate) operands and launch
+struct OzOperand {
+  gc::DevBuf<__nv_bfloat16> buf;
+  gc::DevBuf<int> exps;
+  CUtensorMap map;
+  int rows = 0, Kp = 0, nb = 1, S = 0;
+};
+
+bool is_oz(int precision) { return precision == GC_PREC_FP64TC5 || precision == GC_PREC_FP64TC6; }
+
+OzPlan oz_plan(int precision) {
+  OzPlan p{};
+  p.S = precision == GC_PREC_FP64TC6 ? 6 : 5;
+  int n = 0;
+  for (int d = 0; d < p.S; ++d)
+    for (int t = 0; t <= d; ++t) {
+      p.pa[n] = t;
+      p.pb[n] = d - t;
+      p.pd[n] = d;
+      ++n;
+    }
+  p.npass = n;
+  // exact FP32 partial sums: (S+2) 2^12 c < 2^24 and 2^14 c < 2^24
+  int c = (4096 / (p.S + 2)) / BK * BK;
+  if ((long long)(p.S + 2) * 4096 * c >= (1ll << 24)) c -= BK;
+  p.chunk_kb = c / BK;
+  return p;
+}
+
+int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, int K, int nb,
+                    long long sr, long long sk, long long sb, int S, int box_rows) {
+  op.rows = rows;
+  op.Kp = (K + BK - 1) / BK * BK;
+  op.nb = nb;
+  op.S = S;
+  size_t plane = (size_t)nb * rows * op.Kp;
+  GC_TRY(op.exps.alloc(ctx, (size_t)nb * rows));
+  GC_TRY(op.buf.alloc(ctx, plane * S));
+  {
+    size_t warps = (size_t)nb * rows;
+    unsigned grid = std::min<unsigned>(gc::ceil_div(warps * 32, 256), 152u * 64u);
+    k_row_exponent<<<grid, 256, 0, ctx->stream>>>(x, rows, K, nb, sr, sk, sb, op.exps.p);
+    GC_LAUNCHED(ctx);
+  }
+  if (sk == 1) {
+    unsigned grid = std::min<unsigned>(gc::ceil_div(plane, 256), 152u * 32u);
+    k_slice_planes<<<grid, 256, 0, ctx->stream>>>(x, rows, K, op.Kp, nb, sr, sk, sb, S, op.exps.p,
+                                                   op.buf.p);
+  } else {
+    dim3 grid(gc::ceil_div(rows, 32), gc::ceil_div(op.Kp, 32), nb);
+    k_slice_planes_t<<<grid, dim3(32, 8), 0, ctx->stream>>>(x, rows, K, op.Kp, nb, sr, sk, sb, S,
+                                                             op.exps.p, op.buf.p);
+  }
+  GC_LAUNCHED(ctx);
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
+  cuuint64_t dims[4] = {(cuuint64_t)op.Kp, (cuuint64_t)rows, (cuuint64_t)nb, (cuuint64_t)S};
+  cuuint64_t strides[3] = {(cuuint64_t)op.Kp * 2, (cuuint64_t)rows * op.Kp * 2,
+                           (cuuint64_t)nb * rows * op.Kp * 2};
+  cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = enc(&op.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, op.buf.p, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GC_OK;
+}
+
+size_t oz_smem_bytes() {
+  return 1024 + OZ_STAGES * (size_t)(BM * BK * 2 + OZ_BN * BK * 2) + (2 * OZ_STAGES + 2) * 8 + 16;
+}
+
+template <int S>
+int launch_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N, int nbatch,
+              const OzPlan &pl, const OzEpi &epi) {
+  static std::once_flag once;
+  static cudaError_t cfg = cudaSuccess;
+  std::call_once(once, [] {
+    cfg = cudaFuncSetAttribute(k_tc_gemm_oz<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)oz_smem_bytes());
+  });
+  GC_CUDA(ctx, cfg);
+  dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, OZ_BN), nbatch);
+  k_tc_gemm_oz<S><<<grid, 192, oz_smem_bytes(), ctx->stream>>>(
+      A.map, B.map, M, N, A.Kp / BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag);
+  GC_LAUNCHED(ctx);
+  return GC_OK;
+}
+
+int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N, int nbatch,
+           const OzPlan &pl, OzEpi epi) {
+  if (A.Kp != B.Kp) return gc::set_error(ctx, GC_EINVAL, "oz_gemm: K mismatch");
+  epi.ea = A.exps.p;
+  epi.eb = B.exps.p;
+  epi.ea_sb = A.nb > 1 ? A.rows : 0;
+  epi.eb_sb = B.nb > 1 ? B.rows : 0;
+  return pl.S == 6 ? launch_oz<6>(ctx, A, B, M, N, nbatch, pl, epi)
+                   : launch_oz<5>(ctx, A, B, M, N, nbatch, pl, epi);
+}
+
 }  // namespace
 
 namespace gc {
@@ -449,6 +807,24 @@ int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M
                  long long ostride) {
   if (precision == GC_PREC_FP64)
     return fp64_two_sided(ctx, n, cnt, M, nX, CX, nY, CY, T1, out, ostride);
+  if (is_oz(precision)) {
+    OzPlan pl = oz_plan(precision);
+    {
+      OzOperand A, B;
+      GC_TRY(make_oz_operand(ctx, A, M, n * cnt, n, 1, n, 1, 0, pl.S, BM));
+      GC_TRY(make_oz_operand(ctx, B, CX, nX, n, 1, n, 1, 0, pl.S, OZ_BN));
+      OzEpi e{0, T1, (long long)n * cnt, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+      GC_TRY(run_oz(ctx, A, B, n * cnt, nX, 1, pl, e));
+    }
+    {
+      OzOperand A, B;
+      GC_TRY(make_oz_operand(ctx, A, T1, nX, n, cnt, (long long)n * cnt, 1, n, pl.S, BM));
+      GC_TRY(make_oz_operand(ctx, B, CY, nY, n, 1, n, 1, 0, pl.S, OZ_BN));
+      OzEpi e{0, out, nX, ostride, nullptr, nullptr, nullptr, nullptr, 0, 0};
+      GC_TRY(run_oz(ctx, A, B, nX, nY, cnt, pl, e));
+    }
+    return check_flag(ctx);
+  }
   int S;
   PassList pl = pass_list(precision, &S);
   // step 1: T1[(k,q), x] = sum_p M_k[p, q] CX[p, x]   (T1 column-major, ld = n*cnt)
@@ -479,6 +855,15 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
                                &zero, C, ldc));
     return GC_OK;
   }
+  if (is_oz(precision)) {
+    OzPlan pl = oz_plan(precision);
+    OzOperand a, b;
+    GC_TRY(make_oz_operand(ctx, a, A, m, k, 1, 1, lda, 0, pl.S, BM));
+    GC_TRY(make_oz_operand(ctx, b, B, n, k, 1, 1, ldb, 0, pl.S, OZ_BN));
+    OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+    GC_TRY(run_oz(ctx, a, b, m, n, 1, pl, e));
+    return check_flag(ctx);
+  }
   int S;
   PassList pl = pass_list(precision, &S);
   Operand a, b;
@@ -490,8 +875,41 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
   return check_flag(ctx);
 }
 
+int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const double *A,
+                    long long sam, long long sak, const double *B, long long sbn, long long sbk,
+                    double *C, long long ldc) {
+  if (precision == GC_PREC_FP64 || !is_oz(precision))
+    return set_error(ctx, GC_EINVAL, "gemm_strided: needs a sliced FP64-accurate precision");
+  OzPlan pl = oz_plan(precision);
+  OzOperand a, b;
+  GC_TRY(make_oz_operand(ctx, a, A, M, K, 1, sam, sak, 0, pl.S, BM));
+  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
+  OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+  GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
+  return check_flag(ctx);
+}
+
 int tc_dot_gemm(gc_context *ctx, int precision, int N, const double *Ksym, const double *Y,
                 double *result) {
+  if (is_oz(precision)) {
+    OzPlan pl = oz_plan(precision);
+    OzOperand a, b;
+    GC_TRY(make_oz_operand(ctx, a, Ksym, N, N, 1, N, 1, 0, pl.S, BM));
+    GC_TRY(make_oz_operand(ctx, b, Y, N, N, 1, N, 1, 0, pl.S, OZ_BN));
+    size_t ncta = (size_t)ceil_div(N, BM) * ceil_div(N, OZ_BN);
+    DevBuf<double> part;
+    GC_TRY(part.alloc(ctx, ncta));
+    OzEpi e{1, nullptr, N, 0, Y, part.p, nullptr, nullptr, 0, 0};
+    GC_TRY(run_oz(ctx, a, b, N, N, 1, pl, e));
+    std::vector<double> h(ncta);
+    GC_CUDA(ctx, cudaMemcpyAsync(h.data(), part.p, ncta * sizeof(double), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GC_TRY(check_flag(ctx));
+    double sum = 0.0;
+    for (double v : h) sum += v;
+    *result = sum;
+    return GC_OK;
+  }
   int S;
   PassList pl = pass_list(precision, &S);
   Operand a, b;
@@ -527,8 +945,35 @@ extern "C" int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int
                                double *ms_per_launch) {
   if (!ctx) return GC_EINVAL;
   if (m <= 0 || n <= 0 || k <= 0 || reps <= 0 || !ms_per_launch ||
-      (precision != GC_PREC_BF16X3 && precision != GC_PREC_BF16X6))
+      (precision != GC_PREC_BF16X3 && precision != GC_PREC_BF16X6 && !is_oz(precision)))
     return gc::set_error(ctx, GC_EINVAL, "tc_gemm_time: bad arguments");
+  if (is_oz(precision)) {
+    OzPlan pl = oz_plan(precision);
+    gc::DevBuf<double> a, b, c;
+    GC_TRY(a.alloc(ctx, (size_t)m * k));
+    GC_TRY(b.alloc(ctx, (size_t)n * k));
+    GC_TRY(c.alloc(ctx, (size_t)m * n));
+    GC_CUDA(ctx, cudaMemsetAsync(a.p, 0, (size_t)m * k * 8, ctx->stream));
+    GC_CUDA(ctx, cudaMemsetAsync(b.p, 0, (size_t)n * k * 8, ctx->stream));
+    OzOperand A, B;
+    GC_TRY(make_oz_operand(ctx, A, a.p, m, k, 1, k, 1, 0, pl.S, BM));
+    GC_TRY(make_oz_operand(ctx, B, b.p, n, k, 1, k, 1, 0, pl.S, OZ_BN));
+    OzEpi e{0, c.p, m, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+    GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));
+    cudaEvent_t t0, t1;
+    GC_CUDA(ctx, cudaEventCreate(&t0));
+    GC_CUDA(ctx, cudaEventCreate(&t1));
+    GC_CUDA(ctx, cudaEventRecord(t0, ctx->stream));
+    for (int r = 0; r < reps; ++r) GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));
+    GC_CUDA(ctx, cudaEventRecord(t1, ctx->stream));
+    GC_CUDA(ctx, cudaEventSynchronize(t1));
+    float ms = 0.f;
+    GC_CUDA(ctx, cudaEventElapsedTime(&ms, t0, t1));
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    *ms_per_launch = ms / reps;
+    return check_flag(ctx);
+  }
   int S;
   PassList pl = pass_list(precision, &S);
   gc::DevBuf<double> a, b, c;

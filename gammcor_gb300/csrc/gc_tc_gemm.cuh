@@ -21,6 +21,12 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
 int tc_dot_gemm(gc_context *ctx, int precision, int N, const double *Ksym, const double *Y,
                 double *result);
 
+// C[m + n*ldc] = sum_k A(m,k) B(n,k) with A(m,k) = A[m*sam + k*sak] and
+// B(n,k) = B[n*sbn + k*sbk], on the sliced FP64-accurate tensor-core path.
+int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const double *A,
+                    long long sam, long long sak, const double *B, long long sbn, long long sbk,
+                    double *C, long long ldc);
+
 int fp64_two_sided(gc_context *ctx, int n, int cnt, const double *M, int nX, const double *CX,
                    int nY, const double *CY, double *T1, double *out, long long ostride);
 

@@ -35,8 +35,13 @@ enum gc_status {
 enum gc_precision {
   GC_PREC_FP64 = 0,    /* plain FP64 (cuBLAS DGEMM) */
   GC_PREC_BF16X3 = 1,  /* split-BF16 3-pass on tcgen05 tensor cores, FP32 accumulate */
-  GC_PREC_BF16X6 = 2   /* three BF16 planes, 6 passes (products x_i y_j, i+j<=2): FP32-level
+  GC_PREC_BF16X6 = 2,  /* three BF16 planes, 6 passes (products x_i y_j, i+j<=2): FP32-level
                           product error, tcgen05 tensor cores, FP32 accumulate */
+  GC_PREC_FP64TC5 = 3, /* FP64-accurate on tcgen05: rows scaled by powers of two and cut into
+                          5 integer BF16 slices; products of equal weight accumulate exactly in
+                          FP32 over K chunks short enough to stay below 2^24; chunks summed in
+                          FP64. 15 passes, error ~2^-35 of |A||B|^T */
+  GC_PREC_FP64TC6 = 4  /* as FP64TC5 with 6 slices: 21 passes, error ~2^-42 of |A||B|^T */
 };
 
 /* ERPA eigen-solver form. */

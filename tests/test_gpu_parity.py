@@ -137,7 +137,8 @@ def test_acecorr_n64_golden():
         np.testing.assert_allclose(ws, d["w_lambda"], atol=1e-9)
 
 
-@pytest.mark.parametrize("precision,tol", [("bf16x3", 5e-5), ("bf16x6", 2e-7)])
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 5e-5), ("bf16x6", 2e-7), ("fp64tc5", 1e-10),
+                                           ("fp64tc6", 1e-10)])
 def test_tran4_mixed_precision_error(sys24, precision, tol):
     """Mixed-precision transform vs the FP64 oracle: max |error| per integral."""
     s, G, ffoo, fofo = sys24
@@ -150,7 +151,8 @@ def test_tran4_mixed_precision_error(sys24, precision, tol):
     assert np.abs(gfo2.cpu().numpy() - fofo).max() < tol
 
 
-@pytest.mark.parametrize("precision,tol", [("bf16x3", 1e-4), ("bf16x6", 5e-8)])
+@pytest.mark.parametrize("precision,tol", [("bf16x3", 1e-4), ("bf16x6", 5e-8), ("fp64tc5", 1e-9),
+                                           ("fp64tc6", 1e-9)])
 def test_integrand_mixed_precision_error(sys24, precision, tol):
     s, G, ffoo, fofo = sys24
     indn = R.pair_space(s.occ, s.nele)

@@ -2,7 +2,9 @@
 
 Error bounds, relative to the entries of |A| |B|^T: 3-pass BF16 (hi*hi +
 hi*lo + lo*hi) 2e-5; 6-pass BF16 (three planes) 1e-6 (FP32 accumulation
-dominates).
+dominates); sliced FP64-accurate forms (exact integer partial sums) 5e-10
+with 5 slices and 5e-12 with 6 (truncation after 35 / 42 bits of the row
+maxima; a CPU emulation of the same slicing gives up to 1.5e-10 / 1.2e-12).
 """
 import pytest
 import torch
@@ -10,10 +12,10 @@ import torch
 from gammcor_gb300 import api
 
 pytestmark = pytest.mark.gpu
-BOUND = {"bf16x3": 2e-5, "bf16x6": 1e-6}
+BOUND = {"bf16x3": 2e-5, "bf16x6": 1e-6, "fp64tc5": 5e-10, "fp64tc6": 5e-12}
 
 
-@pytest.mark.parametrize("precision", ["bf16x3", "bf16x6"])
+@pytest.mark.parametrize("precision", ["bf16x3", "bf16x6", "fp64tc5", "fp64tc6"])
 @pytest.mark.parametrize("m,n,k", [(128, 128, 64), (200, 150, 300), (1000, 700, 513),
                                    (7, 300, 40), (640, 90, 1500)])
 def test_tc_gemm_matches_fp64(gpu_lib, precision, m, n, k):
@@ -26,6 +28,21 @@ def test_tc_gemm_matches_fp64(gpu_lib, precision, m, n, k):
     scale = (A.abs() @ B.abs().T)
     err = ((C - ref).abs() / scale).max().item()
     assert err < BOUND[precision], err
+
+
+def test_sliced_gemm_long_k_and_wide_range(gpu_lib):
+    """K spanning many exact chunks, rows 1e12 apart and B rows dominated by a
+    1e6-scaled block (the exact-slicing emulation gives 6.5e-10 / 5.1e-12 here)."""
+    g = torch.Generator(device="cuda").manual_seed(7)
+    A = torch.randn(300, 5000, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(260, 5000, dtype=torch.float64, device="cuda", generator=g)
+    A[::2] *= 1e-12
+    B[:, 100:200] *= 1e6
+    ref = A @ B.T
+    scale = A.abs() @ B.abs().T
+    for prec, bound in (("fp64tc5", 2e-9), ("fp64tc6", 2e-11)):
+        C = api.tc_gemm_nt(A, B, prec)
+        assert ((C - ref).abs() / scale).max().item() < bound
 
 
 def test_tc_gemm_repeated_calls_agree(gpu_lib):
