@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--precision", default="fp64tc5")
     ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--eig-emulation", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -206,7 +207,8 @@ def run_ours(args):
 
     def fast(b):
         return api.ac_energy_batched(b, ngrid=args.ngrid, precision=args.precision,
-                                     erpa_mode="cholesky", affine=True, nstreams=args.nstreams)
+                                     erpa_mode="cholesky", affine=True, nstreams=args.nstreams,
+                                     eig_emulation=bool(args.eig_emulation))
 
     t0 = time.time()
     batch = make_batch(args.nsys, args.seed, dev, fast, rank_offset=rank, log=log)
@@ -306,6 +308,7 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
                            "precision": args.precision, "erpa": "cholesky(A+B), affine A+-B",
                            "streams": args.nstreams, "surrogate": "off",
+                           "eig_emulation": bool(args.eig_emulation),
                            "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"},
                 "plain_fp64_subset": {"systems": sub, "plain_s": t_plain, "fast_s": t_fast_sub,
                                       "speedup": t_plain / t_fast_sub,

@@ -29,7 +29,7 @@ class GcSystem(C.Structure):
 
 class GcAcParams(C.Structure):
     _fields_ = [("ngrid", C.c_int), ("precision", C.c_int), ("erpa_mode", C.c_int),
-                ("affine", C.c_int), ("nstreams", C.c_int)]
+                ("affine", C.c_int), ("nstreams", C.c_int), ("eig_emulation", C.c_int)]
 
 
 # name -> (restype, argtypes); the list mirrors include/gammcor_gpu.h
@@ -39,6 +39,7 @@ SIGNATURES = {
     "gc_last_error": (C.c_char_p, [_vp]),
     "gc_synchronize": (C.c_int, [_vp]),
     "gc_kernel_launches": (C.c_longlong, [_vp]),
+    "gc_set_eig_emulation": (C.c_int, [_vp, C.c_int]),
     "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "gc_prepare_nums": (C.c_int, [C.c_int, _dp, C.c_int, _ip, _ip]),
     "gc_pair_space": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_double, _ip, _ip]),

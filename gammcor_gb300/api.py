@@ -52,6 +52,10 @@ class Context:
     def sync(self):
         check(self.h, load().gc_synchronize(self.h))
 
+    def set_eig_emulation(self, on: bool):
+        """cuSOLVER FP64 emulation strategy for the eigensolver (EAGER when on)."""
+        check(self.h, load().gc_set_eig_emulation(self.h, int(on)))
+
 
 _default: dict[int, Context] = {}
 
@@ -293,13 +297,14 @@ class BatchInputs:
         return [len(x) for x in self.indn]
 
 
-def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "bf16x6",
+def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64tc5",
                       erpa_mode: str = "cholesky", affine: bool = True, nstreams: int = 8,
-                      ctx: Context | None = None):
+                      eig_emulation: bool = False, ctx: Context | None = None):
     """ACECORR over a batch. Returns (ecorr, ecas, W[nsys, ngrid], status)."""
     ctx = ctx or default_context(torch.device(batch.device).index or 0)
     nsys = len(batch.systems)
-    par = _lib.GcAcParams(ngrid, PREC[precision], ERPA[erpa_mode], int(affine), nstreams)
+    par = _lib.GcAcParams(ngrid, PREC[precision], ERPA[erpa_mode], int(affine), nstreams,
+                          int(eig_emulation))
     ecorr = np.zeros(nsys)
     ecas = np.zeros(nsys)
     wl = np.zeros((nsys, ngrid))

@@ -84,6 +84,14 @@ int gc_synchronize(gc_context *ctx) {
 
 long long gc_kernel_launches(const gc_context *ctx) { return ctx ? ctx->launches : 0; }
 
+int gc_set_eig_emulation(gc_context *ctx, int on) {
+  if (!ctx) return GC_EINVAL;
+  GC_CUSOLVER(ctx, cusolverDnSetEmulationStrategy(
+                       ctx->cusolver, on ? CUDA_EMULATION_STRATEGY_EAGER : CUDA_EMULATION_STRATEGY_DEFAULT));
+  ctx->eig_emulation = on ? 1 : 0;
+  return GC_OK;
+}
+
 // misc.f:828-865 (Numerical Recipes gauleg, EPS = 3e-14)
 int gc_gauleg(double x1, double x2, double *x, double *w, int n) {
   if (n <= 0 || !x || !w) return GC_EINVAL;

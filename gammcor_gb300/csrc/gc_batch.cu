@@ -102,6 +102,8 @@ extern "C" int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *
     GC_CUDA(ctx, cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming));
     int r = gc_create(&w.ctx, ctx->device, w.stream);
     if (r != GC_OK) return gc::set_error(ctx, r, "ac_energy_batched: worker context");
+    if (par->eig_emulation && (r = gc_set_eig_emulation(w.ctx, 1)) != GC_OK)
+      return gc::set_error(ctx, r, "ac_energy_batched: %s", w.ctx->err.c_str());
     GC_CUDA(ctx, cudaStreamWaitEvent(w.stream, start, 0));
   }
   std::atomic<int> next{0};

@@ -21,6 +21,7 @@ struct gc_context {
   int *dev_info = nullptr;           // cuSOLVER info slot
   int *dev_flag = nullptr;           // device error flag for bounded waits
   long long launches = 0;            // kernels of this library launched
+  int eig_emulation = 0;             // cuSOLVER FP64 emulation strategy EAGER when 1
   std::string err;
 };
 

@@ -430,14 +430,18 @@ def make_system_device(n: int, nin: int, nact: int, rank: int, seed: int,
         K = torch.einsum('pmi,pni->mn', Y, Y)
         return J, K
 
-    # SCF (same scheme as scf())
+    # SCF (same scheme as scf()); J/K on the device, the n x n eigenproblems on the host
+    def eigh_h(Mt):
+        w, v = np.linalg.eigh(Mt.cpu().numpy())
+        return torch.as_tensor(w, device=dev), torch.as_tensor(v, device=dev)
+
     c = torch.as_tensor(guess, device=dev)
     D = c[:, :nele] @ c[:, :nele].T
     fs, es = [], []
     e_old = None
     it = 0
     for it in range(1, 61):
-        w, v = torch.linalg.eigh(D)
+        w, v = eigh_h(D)
         keep = w > 1e-12
         X = v[:, keep] * torch.sqrt(w[keep])[None, :]
         J, K = jk(D, X)
@@ -453,25 +457,25 @@ def make_system_device(n: int, nin: int, nact: int, rank: int, seed: int,
             es.append(err)
             fs, es = fs[-8:], es[-8:]
             m = len(fs)
-            B = -torch.ones((m + 1, m + 1), dtype=torch.float64, device=dev)
+            B = -np.ones((m + 1, m + 1))
             B[m, m] = 0.0
             for i in range(m):
                 for j in range(m):
-                    B[i, j] = torch.sum(es[i] * es[j])
-            rhs = torch.zeros(m + 1, dtype=torch.float64, device=dev)
+                    B[i, j] = float(torch.sum(es[i] * es[j]))
+            rhs = np.zeros(m + 1)
             rhs[m] = -1.0
             try:
-                coef = torch.linalg.solve(B, rhs)[:m]
-                Fx = sum(ci * fi for ci, fi in zip(coef, fs))
-            except RuntimeError:
+                coef = np.linalg.solve(B, rhs)[:m]
+                Fx = sum(float(ci) * fi for ci, fi in zip(coef, fs))
+            except np.linalg.LinAlgError:
                 Fx = F
-            _, cc = torch.linalg.eigh(Fx)
+            _, cc = eigh_h(Fx)
             D = cc[:, :nele] @ cc[:, :nele].T
         else:
             fs, es = [], []
-            _, cc = torch.linalg.eigh(F + 2.0 * (eye - D))
+            _, cc = eigh_h(F + 2.0 * (eye - D))
             D = 0.5 * D + 0.5 * (cc[:, :nele] @ cc[:, :nele].T)
-    _, cmo_t = torch.linalg.eigh(F)
+    _, cmo_t = eigh_h(F)
 
     # frozen-core CAS-CI
     ccore = cmo_t[:, :nin]

@@ -58,6 +58,10 @@ const char *gc_last_error(const gc_context *ctx);
 int gc_synchronize(gc_context *ctx);
 /* Number of kernels of this library launched on the context so far. */
 long long gc_kernel_launches(const gc_context *ctx);
+/* on = 1 lets cuSOLVER run the FP64 eigensolver's internal matrix products with
+ * its fixed-point FP64 emulation on tensor cores (cusolverDnSetEmulationStrategy
+ * EAGER); on = 0 restores the default. The eigensolver stays an FP64 dsyevd. */
+int gc_set_eig_emulation(gc_context *ctx, int on);
 
 /* Host-side helpers ----------------------------------------------------- */
 
@@ -180,6 +184,7 @@ typedef struct gc_ac_params {
   int erpa_mode;   /* gc_erpa_mode */
   int affine;      /* 1: assemble A+-B at lambda = 0 and 1 once, combine per point */
   int nstreams;    /* concurrent worker streams */
+  int eig_emulation; /* 1: gc_set_eig_emulation on every worker context */
 } gc_ac_params;
 
 /* ACECORR for nsys independent systems (no counterpart in the reference, which
