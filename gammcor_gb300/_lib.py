@@ -29,7 +29,8 @@ class GcSystem(C.Structure):
 
 class GcAcParams(C.Structure):
     _fields_ = [("ngrid", C.c_int), ("precision", C.c_int), ("erpa_mode", C.c_int),
-                ("affine", C.c_int), ("nstreams", C.c_int), ("eig_emulation", C.c_int)]
+                ("affine", C.c_int), ("nstreams", C.c_int), ("eig_emulation", C.c_int),
+                ("lam", _dp), ("weight", _dp)]
 
 
 # name -> (restype, argtypes); the list mirrors include/gammcor_gpu.h
@@ -53,7 +54,15 @@ SIGNATURES = {
     "gc_ace_ne_erpa_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
                                       _vp, C.c_int, _dp]),
     "gc_ac_energy_batched": (C.c_int, [_vp, C.c_int, C.POINTER(GcSystem), C.POINTER(GcAcParams),
-                                       _dp, _dp, _dp, _ip]),
+                                       _dp, _dp, _dp, _dp, _ip]),
+    "gc_mlp_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
+    "gc_mlp_destroy": (C.c_int, [_vp]),
+    "gc_mlp_num_params": (C.c_longlong, [_vp]),
+    "gc_mlp_set_params": (C.c_int, [_vp, _vp, _vp]),
+    "gc_mlp_get_params": (C.c_int, [_vp, _vp, _vp]),
+    "gc_mlp_forward": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp]),
+    "gc_mlp_gradients": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, _vp, C.POINTER(C.c_float)]),
+    "gc_mlp_train_step": (C.c_int, [_vp, _vp, C.c_int, _vp, _vp, C.c_float, C.POINTER(C.c_float)]),
     "gc_tc_gemm_time": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp]),
     "gc_tc_gemm_nt": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int,
                                 _vp, C.c_int]),

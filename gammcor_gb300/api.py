@@ -299,20 +299,34 @@ class BatchInputs:
 
 def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64tc5",
                       erpa_mode: str = "cholesky", affine: bool = True, nstreams: int = 8,
-                      eig_emulation: bool = False, ctx: Context | None = None):
-    """ACECORR over a batch. Returns (ecorr, ecas, W[nsys, ngrid], status)."""
+                      eig_emulation: bool = False, lambdas=None, weights=None,
+                      omega_stats: bool = False, ctx: Context | None = None):
+    """ACECORR over a batch. Returns (ecorr, ecas, W[nsys, npoints], status) and,
+    with omega_stats, the excitation-energy statistics [nsys, npoints, 6].
+    lambdas/weights select explicit quadrature points instead of Gauss-Legendre."""
     ctx = ctx or default_context(torch.device(batch.device).index or 0)
     nsys = len(batch.systems)
+    lam = wts = None
+    if lambdas is not None:
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        ngrid = lam.shape[0]
+        wts = np.ascontiguousarray(weights if weights is not None else np.zeros(ngrid),
+                                   dtype=np.float64)
     par = _lib.GcAcParams(ngrid, PREC[precision], ERPA[erpa_mode], int(affine), nstreams,
-                          int(eig_emulation))
+                          int(eig_emulation), _dptr(lam) if lam is not None else None,
+                          _dptr(wts) if wts is not None else None)
     ecorr = np.zeros(nsys)
     ecas = np.zeros(nsys)
     wl = np.zeros((nsys, ngrid))
+    st = np.zeros((nsys, ngrid, 6)) if omega_stats else None
     status = np.zeros(nsys, dtype=np.int32)
     check(ctx.h, load().gc_ac_energy_batched(ctx.h, nsys, batch.structs, C.byref(par),
-                                             _dptr(ecorr), _dptr(ecas), _dptr(wl), _iptr(status)))
+                                             _dptr(ecorr), _dptr(ecas), _dptr(wl),
+                                             _dptr(st) if st is not None else None,
+                                             _iptr(status)))
+    if omega_stats:
+        return ecorr, ecas, wl, status, st
     return ecorr, ecas, wl, status
-
 
 def tc_gemm_time(m: int, n: int, k: int, precision: str = "bf16x6", reps: int = 10,
                  ctx: Context | None = None) -> float:
@@ -321,3 +335,59 @@ def tc_gemm_time(m: int, n: int, k: int, precision: str = "bf16x6", reps: int = 
     ms = C.c_double()
     check(ctx.h, load().gc_tc_gemm_time(ctx.h, PREC[precision], m, n, k, reps, C.byref(ms)))
     return ms.value
+
+
+# ------------------------------------------------------------------ surrogate
+class Mlp:
+    """The integrand surrogate network, trained and evaluated by this library's kernels."""
+
+    def __init__(self, in_dim: int, hidden: int = 256, out_dim: int = 8, seed: int = 0,
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context(0)
+        self.in_dim, self.hidden, self.out_dim = in_dim, hidden, out_dim
+        h = C.c_void_p()
+        check(self.ctx.h, load().gc_mlp_create(self.ctx.h, in_dim, hidden, out_dim, seed,
+                                               C.byref(h)))
+        self.h = h
+        self.nparam = int(load().gc_mlp_num_params(h))
+
+    def __del__(self):
+        try:
+            if self.h:
+                load().gc_mlp_destroy(self.h)
+        except Exception:
+            pass
+
+    @staticmethod
+    def _dev(x) -> torch.Tensor:
+        return torch.as_tensor(x).to(device="cuda", dtype=torch.float32).contiguous()
+
+    def params(self) -> torch.Tensor:
+        p = torch.empty(self.nparam, dtype=torch.float32, device="cuda")
+        check(self.ctx.h, load().gc_mlp_get_params(self.ctx.h, self.h, _ptr(p)))
+        return p
+
+    def set_params(self, p):
+        p = self._dev(p)
+        check(self.ctx.h, load().gc_mlp_set_params(self.ctx.h, self.h, _ptr(p)))
+
+    def forward(self, x) -> torch.Tensor:
+        x = self._dev(x)
+        y = torch.empty((x.shape[0], self.out_dim), dtype=torch.float32, device="cuda")
+        check(self.ctx.h, load().gc_mlp_forward(self.ctx.h, self.h, x.shape[0], _ptr(x), _ptr(y)))
+        return y
+
+    def gradients(self, x, t):
+        x, t = self._dev(x), self._dev(t)
+        g = torch.empty(self.nparam, dtype=torch.float32, device="cuda")
+        loss = C.c_float()
+        check(self.ctx.h, load().gc_mlp_gradients(self.ctx.h, self.h, x.shape[0], _ptr(x), _ptr(t),
+                                                  _ptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, x, t, lr: float) -> float:
+        x, t = self._dev(x), self._dev(t)
+        loss = C.c_float()
+        check(self.ctx.h, load().gc_mlp_train_step(self.ctx.h, self.h, x.shape[0], _ptr(x), _ptr(t),
+                                                   float(lr), C.byref(loss)))
+        return loss.value

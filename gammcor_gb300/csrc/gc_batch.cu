@@ -24,8 +24,25 @@ struct Worker {
   cudaEvent_t done = nullptr;
 };
 
+void omega_stats(const std::vector<double> &e, double *st) {
+  std::vector<double> k;
+  for (double v : e)
+    if (v > 1e-3 && v < 1e8) k.push_back(v);
+  for (int i = 0; i < GC_OMEGA_STATS; ++i) st[i] = 0.0;
+  if (k.empty()) return;
+  std::sort(k.begin(), k.end());
+  double s = 0, si = 0;
+  for (double v : k) s += v, si += 1.0 / v;
+  st[0] = (double)k.size() / (double)e.size();
+  st[1] = k.front();
+  st[2] = k.back();
+  st[3] = s / k.size();
+  st[4] = si / k.size();
+  st[5] = k[k.size() / 2];
+}
+
 int run_system(gc_context *ctx, const gc_system &s, const gc_ac_params &par, double *ecorr,
-               double *ecas, double *w_out) {
+               double *ecas, double *w_out, double *stats_out) {
   const int n = s.nbas, nocc = s.ninact + s.nact, N = s.ndimx;
   const size_t NN = (size_t)N * N;
   gc::DevBuf<double> ffoo, fofo, co;
@@ -39,8 +56,15 @@ int run_system(gc_context *ctx, const gc_system &s, const gc_ac_params &par, dou
                            par.precision));
   gc::SysDev sd;
   GC_TRY(gc::sys_upload(ctx, sd, n, s.ninact, s.nact, N, s.occ, s.xone, s.indn, s.rdm2act));
-  std::vector<double> x(par.ngrid), w(par.ngrid);
-  gc_gauleg(0.0, 1.0, x.data(), w.data(), par.ngrid);
+  std::vector<double> x(par.ngrid), w(par.ngrid, 0.0);
+  if (par.lambda) {
+    for (int i = 0; i < par.ngrid; ++i) {
+      x[i] = par.lambda[i];
+      w[i] = par.weight ? par.weight[i] : 0.0;
+    }
+  } else {
+    gc_gauleg(0.0, 1.0, x.data(), w.data(), par.ngrid);
+  }
   gc::DevBuf<double> ap, am, Y, eig, a0p, a0m, a1p, a1m;
   GC_TRY(ap.alloc(ctx, NN));
   GC_TRY(am.alloc(ctx, NN));
@@ -68,6 +92,13 @@ int run_system(gc_context *ctx, const gc_system &s, const gc_ac_params &par, dou
     double wi = 0.0;
     GC_TRY(gc::integrand(ctx, sd, Y.p, eig.p, fofo.p, par.precision, &wi));
     if (w_out) w_out[i] = wi;
+    if (stats_out) {
+      std::vector<double> he(N);
+      GC_CUDA(ctx, cudaMemcpyAsync(he.data(), eig.p, N * sizeof(double), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+      GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      omega_stats(he, stats_out + (size_t)i * GC_OMEGA_STATS);
+    }
     acc += w[i] * wi;
   }
   *ecorr = acc;
@@ -79,7 +110,7 @@ int run_system(gc_context *ctx, const gc_system &s, const gc_ac_params &par, dou
 
 extern "C" int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *sys,
                                     const gc_ac_params *par, double *ecorr, double *ecas,
-                                    double *w_lambda, int *status) {
+                                    double *w_lambda, double *omega_st, int *status) {
   if (!ctx) return GC_EINVAL;
   if (nsys <= 0 || !sys || !par || !ecorr || !ecas || par->ngrid <= 0 || par->ngrid > 100)
     return gc::set_error(ctx, GC_EINVAL, "ac_energy_batched: bad arguments");
@@ -117,7 +148,8 @@ extern "C" int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *
       if (k >= nsys || first_err.load() != GC_OK) break;
       int i = order[k];
       int r = run_system(w.ctx, sys[i], *par, &ecorr[i], &ecas[i],
-                         w_lambda ? w_lambda + (size_t)i * par->ngrid : nullptr);
+                         w_lambda ? w_lambda + (size_t)i * par->ngrid : nullptr,
+                         omega_st ? omega_st + (size_t)i * par->ngrid * GC_OMEGA_STATS : nullptr);
       if (status) status[i] = r;
       if (r != GC_OK && !(status && r == GC_ENOTPD)) {
         int expected = GC_OK;

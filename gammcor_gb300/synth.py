@@ -509,7 +509,9 @@ def make_system_device(n: int, nin: int, nact: int, rank: int, seed: int,
         _, uv = np.linalg.eigh(fmo[nocc:, nocc:])
         cmo[:, nocc:] = cmo[:, nocc:] @ uv
     xone = pack_sym(cmo.T @ h @ cmo)
+    cmt = torch.as_tensor(cmo, device=dev)
+    fdiag = torch.diagonal(cmt.T @ (H + 2 * J - K) @ cmt).cpu().numpy()  # CAS Fock diagonal
     del Lsq
     return System(n=n, nin=nin, nact=nact, rank=rank, seed=seed, lfac=lfac, h_ao=h,
                   cmo=cmo, occ=occ, xone=xone, rdm2act=pack_rdm2act(g2no),
-                  e_cas=e_cas, nele=nele, extra=dict(e_scf=e, scf_iter=it))
+                  e_cas=e_cas, nele=nele, extra=dict(e_scf=e, scf_iter=it, fock_diag=fdiag))

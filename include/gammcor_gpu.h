@@ -185,16 +185,44 @@ typedef struct gc_ac_params {
   int affine;      /* 1: assemble A+-B at lambda = 0 and 1 once, combine per point */
   int nstreams;    /* concurrent worker streams */
   int eig_emulation; /* 1: gc_set_eig_emulation on every worker context */
+  const double *lambda;  /* host, ngrid points; NULL: Gauss-Legendre points on [0,1] */
+  const double *weight;  /* host, ngrid weights used with lambda (NULL: all zero) */
 } gc_ac_params;
+
+/* Per system and lambda point, statistics of the ERPA excitation energies kept by
+ * the integrand (1e-3 < omega < 1e8): fraction kept, min, max, mean, mean of
+ * 1/omega, median. */
+#define GC_OMEGA_STATS 6
 
 /* ACECORR for nsys independent systems (no counterpart in the reference, which
  * runs one system per process). ecorr/ecas (nsys), w_lambda (nsys*ngrid, may be
- * NULL). status (nsys, may be NULL): per-system gc_status; when given, systems
- * with A+B not positive definite (GC_ENOTPD) are reported there instead of
- * failing the call. */
+ * NULL), omega_stats (nsys*ngrid*GC_OMEGA_STATS, may be NULL). status (nsys, may
+ * be NULL): per-system gc_status; when given, systems with A+B not positive
+ * definite (GC_ENOTPD) are reported there instead of failing the call. */
 int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *sys,
                          const gc_ac_params *par, double *ecorr, double *ecas,
-                         double *w_lambda, int *status);
+                         double *w_lambda, double *omega_stats, int *status);
+
+/* Integrand surrogate (no counterpart in the reference) ---------------------
+ * Multilayer perceptron in -> H -> H -> H -> out with GELU on the hidden layers,
+ * BF16 weights in the forward pass, FP32 accumulation, FP32 master weights and
+ * Adam moments for training. Parameters flattened as W1 (H x in), b1, W2 (H x H),
+ * b2, W3 (H x H), b3, W4 (out x H), b4, row-major. x_dev (batch x in), targets
+ * and outputs (batch x out) are row-major FP32 device arrays. */
+typedef struct gc_mlp gc_mlp;
+int gc_mlp_create(gc_context *ctx, int in_dim, int hidden, int out_dim,
+                  unsigned long long seed, gc_mlp **mlp);
+int gc_mlp_destroy(gc_mlp *mlp);
+long long gc_mlp_num_params(const gc_mlp *mlp);
+int gc_mlp_set_params(gc_context *ctx, gc_mlp *mlp, const float *params_dev);
+int gc_mlp_get_params(gc_context *ctx, gc_mlp *mlp, float *params_dev);
+int gc_mlp_forward(gc_context *ctx, gc_mlp *mlp, int batch, const float *x_dev, float *y_dev);
+/* Mean-squared-error loss and its gradient w.r.t. the parameters (grad_dev may be NULL). */
+int gc_mlp_gradients(gc_context *ctx, gc_mlp *mlp, int batch, const float *x_dev,
+                     const float *t_dev, float *grad_dev, float *loss_host);
+/* One Adam step (beta 0.9 / 0.999) on the MSE loss of the batch. */
+int gc_mlp_train_step(gc_context *ctx, gc_mlp *mlp, int batch, const float *x_dev,
+                      const float *t_dev, float lr, float *loss_host);
 
 /* Building block ---------------------------------------------------------- */
 
