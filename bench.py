@@ -8,9 +8,11 @@ resident in HBM for `value`; `e2e` copies them from pinned host memory inside
 the timed region. The per-system working set (ERI factor, FFOO/FOFO, A+-B) is
 larger than L2 for all but the smallest systems.
 
-The fast form (FP64-accurate sliced-BF16 tensor-core transform, ERPA products
-and integrand, Cholesky ERPA on an affine A+-B, concurrent worker streams) is
-timed for `value`; the plain FP64
+The measured step is the mixed + batched + learned form: FP64-accurate
+sliced-BF16 tensor-core transform, ERPA products and integrand, Cholesky ERPA on
+an affine A+-B, concurrent worker streams, and the integrand surrogate (ERPA at
+the two end nodes of the 8-point rule, an ensemble estimate, and the six
+interior nodes where the estimate exceeds 1 microhartree); the plain FP64
 GPU path (ERPASYMM1, A+-B reassembled per point, one stream) is timed on every
 8th system together with the fast form on the same systems, and every fast
 energy of that subset is checked against the plain FP64 energy (1 microhartree).
@@ -50,7 +52,13 @@ def parse():
     ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--eig-emulation", type=int, default=0)
-    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--surrogate", type=int, default=1)
+    ap.add_argument("--threshold", type=float, default=1e-6)
+    ap.add_argument("--gen", default="device", choices=["device", "cpu"],
+                    help="input generator: FP64 torch on the GPU, or numpy on the host")
+    ap.add_argument("--no-subset", action="store_true")
+    ap.add_argument("--kernel-only", type=int, default=0,
+                    help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
 
@@ -120,15 +128,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_batch(nsys, seed, device, run, rank_offset=0, log=print):
+def make_batch(nsys, seed, device, run, rank_offset=0, log=print, gen="device"):
     """Generate the batch. Systems whose A+B is not positive definite at a
     quadrature point are reported by the GPU path itself (Cholesky status) and
     resampled; the final check run is the first warm-up step on the final batch."""
     from gammcor_gb300 import api, synth
     shapes = synth.batched_shapes(count=nsys, seed=seed + 7919 * rank_offset)
+    if gen == "device":
+        make = lambda n, a, b, r, sd: synth.make_system_device(n, a, b, r, sd, device=device)  # noqa
+    else:
+        make = lambda n, a, b, r, sd: synth.make_system(n, a, b, r, sd)  # noqa
     t0 = time.time()
-    systems = [synth.make_system_device(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"],
-                                        device=device) for sh in shapes]
+    systems = [make(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"]) for sh in shapes]
     log(f"generated {nsys} systems in {time.time() - t0:.1f}s")
     for attempt in range(1, 8):
         batch = api.BatchInputs(systems, device=device)
@@ -139,8 +150,8 @@ def make_batch(nsys, seed, device, run, rank_offset=0, log=print):
         log(f"resampling {len(bad)} systems (A+B not positive definite): {bad}")
         for i in bad:
             sh = shapes[i]
-            systems[i] = synth.make_system_device(sh["n"], sh["nin"], sh["nact"], sh["rank"],
-                                                  sh["seed"] + 100000 * attempt, device=device)
+            systems[i] = make(sh["n"], sh["nin"], sh["nact"], sh["rank"],
+                              sh["seed"] + 100000 * attempt)
     raise RuntimeError("could not find positive-definite systems")
 
 
@@ -203,15 +214,28 @@ def run_ours(args):
 
     import __graft_entry__
     __graft_entry__.build()
-    from gammcor_gb300 import api
+    from gammcor_gb300 import api, surrogate
 
-    def fast(b):
-        return api.ac_energy_batched(b, ngrid=args.ngrid, precision=args.precision,
-                                     erpa_mode="cholesky", affine=True, nstreams=args.nstreams,
-                                     eig_emulation=bool(args.eig_emulation))
+    if args.kernel_only:
+        n = args.kernel_only
+        ms_k = api.tc_gemm_time(n, n, n, args.precision, reps=3)
+        print(json.dumps({"kernel": f"tcgen05 GEMM {args.precision} {n}^3", "ms_per_launch": ms_k}))
+        return
+
+    ens = surrogate.Ensemble.load(surrogate.MODEL) if args.surrogate else None
+    kw = dict(nstreams=args.nstreams, precision=args.precision,
+              eig_emulation=bool(args.eig_emulation))
+
+    def step(b):
+        """One pass over a batch: (energies, fallback mask, error estimate, status)."""
+        if ens is not None:
+            return surrogate.energies(b, ens, threshold=args.threshold, **kw)
+        e, _, _, st = api.ac_energy_batched(b, ngrid=args.ngrid, erpa_mode="cholesky",
+                                            affine=True, **kw)
+        return e, np.ones(len(e), bool), np.zeros(len(e)), st
 
     t0 = time.time()
-    batch = make_batch(args.nsys, args.seed, dev, fast, rank_offset=rank, log=log)
+    batch = make_batch(args.nsys, args.seed, dev, step, rank_offset=rank, log=log, gen=args.gen)
     log(f"batch ready in {time.time() - t0:.1f}s (includes the first warm-up step)")
     ctx = api.default_context(local)
     Ns = batch.ndimx()
@@ -223,64 +247,64 @@ def run_ours(args):
             torch.distributed.barrier()
 
     for _ in range(max(0, args.warmup - 1)):
-        fast(batch)
+        step(batch)
+    # Timed steps. Each step first copies the inputs (MO coefficients, ERI
+    # factors) from pinned host memory (e2e); `value` is timed from the end of
+    # those copies, with the inputs resident in HBM.
+    host_c = [t.cpu().pin_memory() for t in batch.cmo]
+    host_l = [t.cpu().pin_memory() for t in batch.lfac]
+    h2d = sum(t.numel() * 8 for t in host_c) + sum(t.numel() * 8 for t in host_l)
+    d2h = args.nsys * 8 * 2
     barrier()
     stream = torch.cuda.current_stream()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = ctx.launches()
+    ms = ems = 0.0
     with ClockSampler(local) as clk:
-        ev0.record(stream)
         for _ in range(args.steps):
-            ecorr, ecas, wl, status = fast(batch)
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    launches = (ctx.launches() - l0) // args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.nsys / (ms / 1000.0)
-    log(f"fast: {ms:.0f} ms per step, {value:.3f} energies/s, {launches} kernels/step")
-
-    # plain FP64 GPU path and fast form on the same subset; error check
-    sub = list(range(0, args.nsys, args.subset_stride))
-    sb = api.BatchInputs([batch.systems[i] for i in sub], device=dev)
-    api.ac_energy_batched(sb, ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
-                          nstreams=1)  # warm-up of the plain configuration
-    torch.cuda.synchronize()
-    t0 = time.time()
-    pe, pcas, pw, _ = api.ac_energy_batched(sb, ngrid=args.ngrid, precision="fp64",
-                                            erpa_mode="symm1", affine=False, nstreams=1)
-    torch.cuda.synchronize()
-    t_plain = time.time() - t0
-    t0 = time.time()
-    fe, fcas, fw, _ = fast(sb)
-    torch.cuda.synchronize()
-    t_fast_sub = time.time() - t0
-    err = np.abs(fe - pe)
-    log(f"subset {sub}: plain FP64 {t_plain:.1f}s, fast {t_fast_sub:.1f}s, max |dE| {err.max():.2e}")
-
-    # e2e: inputs from pinned host memory every step, energies back to host
-    e2e = None
-    if not args.no_e2e:
-        host_c = [t.cpu().pin_memory() for t in batch.cmo]
-        host_l = [t.cpu().pin_memory() for t in batch.lfac]
-        h2d = sum(t.numel() * 8 for t in host_c) + sum(t.numel() * 8 for t in host_l)
-        d2h = args.nsys * (2 + args.ngrid) * 8
-        barrier()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
             for i in range(args.nsys):
                 batch.cmo[i].copy_(host_c[i], non_blocking=True)
                 batch.lfac[i].copy_(host_l[i], non_blocking=True)
-            fast(batch)
-        e1.record(stream)
-        barrier()
-        ems = e0.elapsed_time(e1) / args.steps
-        e2e = {"value": world * args.nsys / (ems / 1000.0), "unit": "energies/s",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+            e1.record(stream)
+            ecorr, fb, est, status = step(batch)
+            e2.record(stream)
+            barrier()
+            ms += e1.elapsed_time(e2)
+            ems += e0.elapsed_time(e2)
+    ms /= args.steps
+    ems /= args.steps
+    launches = (ctx.launches() - l0) // args.steps
+    if world > 1:
+        t = torch.tensor([ms, ems], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, ems = float(t[0]), float(t[1])
+    value = world * args.nsys / (ms / 1000.0)
+    e2e = {"value": world * args.nsys / (ems / 1000.0), "unit": "energies/s",
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    log(f"step: {ms:.0f} ms, {value:.3f} energies/s (e2e {e2e['value']:.3f}), fallback "
+        f"{fb.mean():.2f}, {launches} kernels/step")
+
+    # plain FP64 GPU path and the measured step on the same subset; error check
+    sub, t_plain, t_fast_sub, err = [], float("nan"), float("nan"), np.zeros(1)
+    if not args.no_subset:
+        sub = list(range(0, args.nsys, args.subset_stride))
+        sb = batch.subset(sub)
+        plain = dict(ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
+                     nstreams=1)
+        api.ac_energy_batched(sb, **plain)  # warm-up of the plain configuration
+        torch.cuda.synchronize()
+        t0 = time.time()
+        pe = api.ac_energy_batched(sb, **plain)[0]
+        torch.cuda.synchronize()
+        t_plain = time.time() - t0
+        t0 = time.time()
+        fe = step(sb)[0]
+        torch.cuda.synchronize()
+        t_fast_sub = time.time() - t0
+        err = np.abs(fe - pe)
+        log(f"subset {sub}: plain FP64 {t_plain:.1f}s, measured step {t_fast_sub:.1f}s, "
+            f"max |dE| {err.max():.2e}")
 
     # roofline of this library's dominant kernel: the tcgen05 GEMM at the
     # integrand shape of the largest system (N x N x N), timed alone
@@ -307,10 +331,13 @@ def run_ours(args):
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
                            "precision": args.precision, "erpa": "cholesky(A+B), affine A+-B",
-                           "streams": args.nstreams, "surrogate": "off",
+                           "streams": args.nstreams,
+                           "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens
+                                         else "off"),
                            "eig_emulation": bool(args.eig_emulation),
                            "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"},
-                "plain_fp64_subset": {"systems": sub, "plain_s": t_plain, "fast_s": t_fast_sub,
+                "surrogate_fallback_rate": float(fb.mean()),
+                "plain_fp64_subset": {"systems": sub, "plain_s": t_plain, "step_s": t_fast_sub,
                                       "speedup": t_plain / t_fast_sub,
                                       "max_abs_err_eh": float(err.max()),
                                       "within_1ueh": bool(err.max() <= 1e-6)},

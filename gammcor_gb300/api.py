@@ -288,6 +288,21 @@ class BatchInputs:
             st.occ, st.xone, st.indn, st.rdm2act = _dptr(occ), _dptr(xone), _iptr(ind), _dptr(rdm)
         self.refresh_pointers()
 
+    def subset(self, idx) -> "BatchInputs":
+        """A batch of some of these systems that shares their device buffers."""
+        sub = BatchInputs.__new__(BatchInputs)
+        idx = [int(i) for i in idx]
+        sub.systems = [self.systems[i] for i in idx]
+        sub.device = self.device
+        sub.cmo = [self.cmo[i] for i in idx]
+        sub.lfac = [self.lfac[i] for i in idx]
+        sub._host = [self._host[i] for i in idx]
+        sub.indn = [self.indn[i] for i in idx]
+        sub.structs = (_lib.GcSystem * len(idx))()
+        for k, i in enumerate(idx):
+            sub.structs[k] = self.structs[i]
+        return sub
+
     def refresh_pointers(self):
         for i in range(len(self.systems)):
             self.structs[i].cmo_dev = self.cmo[i].data_ptr()

@@ -173,6 +173,36 @@ def evaluate(ens: Ensemble, data, thresholds=(1e-6, 1e-5, 1e-4, 1e-3)):
     return res
 
 
+MODEL = __import__("pathlib").Path(__file__).resolve().parent / "data" / "surrogate_ensemble.npz"
+
+
+def energies(batch, ens: Ensemble, threshold: float = 1e-6, nstreams: int = 8,
+             precision: str = "fp64tc5", eig_emulation: bool = False):
+    """AC-CAS energies of a batch with the surrogate: ERPA at the two end nodes
+    for every system, the ensemble's prediction where its error estimate is at
+    most `threshold`, and the six interior nodes (reusing the end nodes) where
+    it is not. Returns (energies, fallback mask, estimate, status)."""
+    x8, w8 = gauss8()
+    ends = list(END)
+    kw = dict(nstreams=nstreams, precision=precision, eig_emulation=eig_emulation)
+    ea, _, wa, st, om = api.ac_energy_batched(batch, lambdas=x8[ends], weights=w8[ends],
+                                              omega_stats=True, **kw)
+    nd = batch.ndimx()
+    X = np.array([features(s, wa[i], om[i], nd[i]) for i, s in enumerate(batch.systems)])
+    e_pred, e_est = estimate(ens, X, wa, w8)
+    fb = ~(e_est <= threshold) | (st != 0)
+    e = e_pred.copy()
+    if fb.any():
+        idx = np.nonzero(fb)[0]
+        inner = list(INNER)
+        eb, _, _, stb = api.ac_energy_batched(batch.subset(idx), lambdas=x8[inner],
+                                              weights=w8[inner], **kw)
+        e[idx] = ea[idx] + eb
+        st = st.copy()
+        st[idx] = np.maximum(st[idx], stb)
+    return e, fb, e_est, st
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser(description="train and evaluate the integrand surrogate")
