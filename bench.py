@@ -10,9 +10,11 @@ larger than L2 for all but the smallest systems.
 
 The measured step is the mixed + batched + learned form: FP64-accurate
 sliced-BF16 tensor-core transform, ERPA products and integrand, Cholesky ERPA on
-an affine A+-B, concurrent worker streams, and the integrand surrogate (ERPA at
-the two end nodes of the 8-point rule, an ensemble estimate, and the six
-interior nodes where the estimate exceeds 1 microhartree); the plain FP64
+an affine A+-B with the eigensolve in FP32 refined to FP64 accuracy, concurrent
+worker streams, and the integrand surrogate (ERPA at the two end nodes of the
+8-point rule, an ensemble estimate, and the six interior nodes where the
+estimate exceeds 1 microhartree, on integrals and A+-B kept on the device by a
+batch session between the two passes); the plain FP64
 GPU path (ERPASYMM1, A+-B reassembled per point, one stream) is timed on every
 8th system together with the fast form on the same systems, and every fast
 energy of that subset is checked against the plain FP64 energy (1 microhartree).
@@ -52,6 +54,10 @@ def parse():
     ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--eig-emulation", type=int, default=0)
+    ap.add_argument("--erpa", default="refined", choices=["cholesky", "refined"],
+                    help="ERPA form of the measured step: FP64 dsyevd of L^T A- L, or an FP32 "
+                         "eigensolve refined to FP64 accuracy")
+    ap.add_argument("--eig-refine", type=int, default=2)
     ap.add_argument("--surrogate", type=int, default=1)
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--gen", default="device", choices=["device", "cpu"],
@@ -224,14 +230,15 @@ def run_ours(args):
 
     ens = surrogate.Ensemble.load(surrogate.MODEL) if args.surrogate else None
     kw = dict(nstreams=args.nstreams, precision=args.precision,
-              eig_emulation=bool(args.eig_emulation))
+              eig_emulation=bool(args.eig_emulation), erpa_mode=args.erpa)
 
     def step(b):
         """One pass over a batch: (energies, fallback mask, error estimate, status)."""
         if ens is not None:
-            return surrogate.energies(b, ens, threshold=args.threshold, **kw)
-        e, _, _, st = api.ac_energy_batched(b, ngrid=args.ngrid, erpa_mode="cholesky",
-                                            affine=True, **kw)
+            return surrogate.energies(b, ens, threshold=args.threshold,
+                                      eig_refine=args.eig_refine, **kw)
+        e, _, _, st = api.ac_energy_batched(b, ngrid=args.ngrid, affine=True,
+                                            eig_refine=args.eig_refine, **kw)
         return e, np.ones(len(e), bool), np.zeros(len(e)), st
 
     t0 = time.time()
@@ -330,7 +337,10 @@ def run_ours(args):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
                 "config": {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
-                           "precision": args.precision, "erpa": "cholesky(A+B), affine A+-B",
+                           "precision": args.precision, "erpa": ("cholesky(A+B), affine A+-B, " +
+                                    ("FP32 eigensolve refined to FP64 accuracy "
+                                     f"({args.eig_refine} iteration(s))"
+                                     if args.erpa == "refined" else "FP64 dsyevd")),
                            "streams": args.nstreams,
                            "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens
                                          else "off"),
@@ -342,7 +352,8 @@ def run_ours(args):
                                       "max_abs_err_eh": float(err.max()),
                                       "within_1ueh": bool(err.max() <= 1e-6)},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk.summary(), "failed_systems": int((status != 0).sum())}
+                "clocks": clk.summary(), "failed_systems": int((status != 0).sum()),
+                "eig_refine_stats": ctx.eig_refine_stats()}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

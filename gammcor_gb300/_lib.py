@@ -15,7 +15,7 @@ GC_OK = 0
 STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "GC_ECUSOLVER",
                 5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED"}
 PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "fp64tc5": 3, "fp64tc6": 4}
-ERPA = {"symm1": 0, "cholesky": 1}
+ERPA = {"symm1": 0, "cholesky": 1, "refined": 2}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -30,7 +30,7 @@ class GcSystem(C.Structure):
 class GcAcParams(C.Structure):
     _fields_ = [("ngrid", C.c_int), ("precision", C.c_int), ("erpa_mode", C.c_int),
                 ("affine", C.c_int), ("nstreams", C.c_int), ("eig_emulation", C.c_int),
-                ("lam", _dp), ("weight", _dp)]
+                ("eig_refine", C.c_int), ("lam", _dp), ("weight", _dp)]
 
 
 # name -> (restype, argtypes); the list mirrors include/gammcor_gpu.h
@@ -41,6 +41,9 @@ SIGNATURES = {
     "gc_synchronize": (C.c_int, [_vp]),
     "gc_kernel_launches": (C.c_longlong, [_vp]),
     "gc_set_eig_emulation": (C.c_int, [_vp, C.c_int]),
+    "gc_set_eig_refinement": (C.c_int, [_vp, C.c_int]),
+    "gc_eig_refine_stats": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_int)]),
     "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "gc_prepare_nums": (C.c_int, [C.c_int, _dp, C.c_int, _ip, _ip]),
     "gc_pair_space": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_double, _ip, _ip]),
@@ -51,10 +54,15 @@ SIGNATURES = {
     "gc_ab_cas_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp,
                                  _vp, C.c_double, _vp, _vp, _dp]),
     "gc_erpa": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int]),
+    "gc_erpa_ex": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int]),
     "gc_ace_ne_erpa_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
                                       _vp, C.c_int, _dp]),
     "gc_ac_energy_batched": (C.c_int, [_vp, C.c_int, C.POINTER(GcSystem), C.POINTER(GcAcParams),
                                        _dp, _dp, _dp, _dp, _ip]),
+    "gc_ac_session_create": (C.c_int, [_vp, C.c_int, C.POINTER(GcSystem), C.POINTER(GcAcParams),
+                                       C.POINTER(C.c_void_p)]),
+    "gc_ac_session_points": (C.c_int, [_vp, C.c_int, _ip, C.c_int, _dp, _dp, _dp, _dp, _ip]),
+    "gc_ac_session_destroy": (C.c_int, [_vp]),
     "gc_mlp_create": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]),
     "gc_mlp_destroy": (C.c_int, [_vp]),
     "gc_mlp_num_params": (C.c_longlong, [_vp]),

@@ -53,8 +53,19 @@ class Context:
         check(self.h, load().gc_synchronize(self.h))
 
     def set_eig_emulation(self, on: bool):
-        """cuSOLVER FP64 emulation strategy for the eigensolver (EAGER when on)."""
+        """cuSOLVER FP64 emulation strategy for the eigensolver (EAGER when on) and
+        BF16x9 math for the FP32 eigensolver of the refined ERPA form."""
         check(self.h, load().gc_set_eig_emulation(self.h, int(on)))
+
+    def set_eig_refinement(self, iterations: int):
+        """Refinement iterations of the refined ERPA form (1..4)."""
+        check(self.h, load().gc_set_eig_refinement(self.h, int(iterations)))
+
+    def eig_refine_stats(self) -> dict:
+        """Refined ERPA counters: solves, dsyevd fallbacks, largest block cluster."""
+        s, f, m = C.c_longlong(), C.c_longlong(), C.c_int()
+        check(self.h, load().gc_eig_refine_stats(self.h, C.byref(s), C.byref(f), C.byref(m)))
+        return {"solves": s.value, "fallbacks": f.value, "max_cluster": m.value}
 
 
 _default: dict[int, Context] = {}
@@ -179,17 +190,21 @@ def ab_cas_fofo(occ: np.ndarray, xone: np.ndarray, indn: np.ndarray, nact: int, 
 
 
 def erpasymm1(abplus: torch.Tensor, abmin: torch.Tensor, mode: str = "symm1",
-              ctx: Context | None = None):
-    """ERPASYMM1 (interpa.f:1652-1781) or its Cholesky form. abplus/abmin are
+              precision: str = "fp64", ctx: Context | None = None):
+    """ERPASYMM1 (interpa.f:1652-1781) or its Cholesky forms ("cholesky",
+    "refined": FP32 eigensolve refined to FP64 accuracy). abplus/abmin are
     Fortran-meaning (N, N) matrices (column-major storage, e.g. the views
-    returned by ab_cas_fofo). Returns (EigVecR, Eig) with EigVecR[:, nu] = Y_nu."""
+    returned by ab_cas_fofo). precision ("fp64", "fp64tc5", "fp64tc6") is the
+    arithmetic of the Cholesky forms' matrix products. Returns (EigVecR, Eig)
+    with EigVecR[:, nu] = Y_nu."""
     ctx = ctx or default_context(abplus.device.index or 0)
     ap = abplus.t().contiguous()   # column-major storage
     am = abmin.t().contiguous()
     N = ap.shape[0]
     y = torch.empty_like(ap)
     eig = torch.empty(N, dtype=torch.float64, device=ap.device)
-    check(ctx.h, load().gc_erpa(ctx.h, N, _ptr(ap), _ptr(am), _ptr(y), _ptr(eig), ERPA[mode]))
+    check(ctx.h, load().gc_erpa_ex(ctx.h, N, _ptr(ap), _ptr(am), _ptr(y), _ptr(eig), ERPA[mode],
+                                   PREC[precision]))
     return y.t(), eig
 
 
@@ -315,7 +330,7 @@ class BatchInputs:
 def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64tc5",
                       erpa_mode: str = "cholesky", affine: bool = True, nstreams: int = 8,
                       eig_emulation: bool = False, lambdas=None, weights=None,
-                      omega_stats: bool = False, ctx: Context | None = None):
+                      omega_stats: bool = False, eig_refine: int = 0, ctx: Context | None = None):
     """ACECORR over a batch. Returns (ecorr, ecas, W[nsys, npoints], status) and,
     with omega_stats, the excitation-energy statistics [nsys, npoints, 6].
     lambdas/weights select explicit quadrature points instead of Gauss-Legendre."""
@@ -328,7 +343,8 @@ def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64
         wts = np.ascontiguousarray(weights if weights is not None else np.zeros(ngrid),
                                    dtype=np.float64)
     par = _lib.GcAcParams(ngrid, PREC[precision], ERPA[erpa_mode], int(affine), nstreams,
-                          int(eig_emulation), _dptr(lam) if lam is not None else None,
+                          int(eig_emulation), int(eig_refine),
+                          _dptr(lam) if lam is not None else None,
                           _dptr(wts) if wts is not None else None)
     ecorr = np.zeros(nsys)
     ecas = np.zeros(nsys)
@@ -342,6 +358,56 @@ def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64
     if omega_stats:
         return ecorr, ecas, wl, status, st
     return ecorr, ecas, wl, status
+
+class AcSession:
+    """Batch with per-system device state kept between calls (gc_ac_session_*):
+    points(idx, lambdas) evaluates W(lambda) for some systems, building a
+    system's integrals and A+-B at lambda = 0, 1 on its first use only."""
+
+    def __init__(self, batch: BatchInputs, precision: str = "fp64tc5",
+                 erpa_mode: str = "refined", nstreams: int = 8, eig_emulation: bool = False,
+                 eig_refine: int = 0, ctx: Context | None = None):
+        self.ctx = ctx or default_context(torch.device(batch.device).index or 0)
+        self.batch = batch  # keeps the host arrays and device buffers alive
+        par = _lib.GcAcParams(0, PREC[precision], ERPA[erpa_mode], 1, nstreams,
+                              int(eig_emulation), int(eig_refine), None, None)
+        h = C.c_void_p()
+        check(self.ctx.h, load().gc_ac_session_create(self.ctx.h, len(batch.systems),
+                                                      batch.structs, C.byref(par), C.byref(h)))
+        self.h = h
+
+    def points(self, idx, lambdas, omega_stats: bool = False):
+        """W[len(idx), len(lambdas)], E_CAS[len(idx)], status[len(idx)] (and the
+        excitation statistics [len(idx), len(lambdas), 6] with omega_stats)."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        w = np.zeros((idx.size, lam.size))
+        st = np.zeros((idx.size, lam.size, 6)) if omega_stats else None
+        ecas = np.zeros(idx.size)
+        status = np.zeros(idx.size, dtype=np.int32)
+        check(self.ctx.h, load().gc_ac_session_points(self.h, idx.size, _iptr(idx), lam.size,
+                                                      _dptr(lam), _dptr(w),
+                                                      _dptr(st) if st is not None else None,
+                                                      _dptr(ecas), _iptr(status)))
+        return (w, ecas, status, st) if omega_stats else (w, ecas, status)
+
+    def close(self):
+        if self.h:
+            load().gc_ac_session_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 def tc_gemm_time(m: int, n: int, k: int, precision: str = "bf16x6", reps: int = 10,
                  ctx: Context | None = None) -> float:

@@ -182,7 +182,7 @@ int gc_acecorr(gc_context *ctx, int nbas, int ninact, int nact, int ndimx, const
   GC_TRY(am.alloc(ctx, NN));
   GC_TRY(Y.alloc(ctx, NN));
   GC_TRY(eig.alloc(ctx, ndimx));
-  const bool affine = erpa_mode == GC_ERPA_CHOLESKY;
+  const bool affine = erpa_mode == GC_ERPA_CHOLESKY || erpa_mode == GC_ERPA_CHOLESKY_REFINED;
   double e0 = 0.0;
   if (affine) {
     GC_TRY(a0p.alloc(ctx, NN));

@@ -105,6 +105,548 @@ int syevd(gc_context *ctx, int N, double *A, double *w) {
   return GC_OK;
 }
 
+
+// ---- FP32 eigensolve refined to FP64 accuracy --------------------------------
+//
+// M = L^T A- L is diagonalised in FP32 (ssyevd on M rounded to FP32); the FP32
+// eigenvectors X are then refined against the FP64 M. One iteration forms
+//   G = X^T X,  S = X^T (M X),  lambda_i = S_ii / G_ii,
+// groups indices into clusters (maximal runs of neighbours k, k+1 whose Rayleigh
+// quotients differ by at most max(c_k, c_k+1) / kTau, c_j the largest coupling
+// |S_ij - (lambda_i + lambda_j) / 2 G_ij| of column j),
+// diagonalises each cluster block exactly in FP64 (Cholesky of G_CC, cyclic Jacobi,
+// back-substitution: V_C^T G_CC V_C = I, V_C^T S_CC V_C diagonal), rotates G and S
+// by the block-diagonal V, and updates
+//   X <- X V (I + E),  E_ij = (S'_ij - lambda'_j G'_ij) / (lambda'_j - lambda'_i)
+// across clusters and E = (I - G') / 2 inside them (first order in the residual,
+// so every cross-cluster |E_ij| <= kTau), with the second-order term -E E^T / 2
+// added to I + E so that the update keeps X orthonormal to third order. This is
+// the iterative refinement of Ogita and Aishima (Japan J. Indust. Appl. Math. 35,
+// 2018) with the clustered eigenvalues treated as exact small blocks. The
+// eigenvalues returned are the Rayleigh quotients of the updated vectors to second
+// order in E (an O(N^2) reduction; the quotients before the update inherit the
+// FP32 vectors' error squared, ~1e-6 relative on cuSOLVER's ssyevd output).
+// W(lambda) depends on the eigenvectors only through sum_nu f(omega_nu) y_nu y_nu^T,
+// so rotations inside a cluster of (near-)equal eigenvalues do not matter; the
+// block solve only has to be exact.
+constexpr int kMaxCluster = 64;
+constexpr double kTau = 0.05;
+
+__global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+__global__ void k_f2d(size_t n, const float *__restrict__ a, double *__restrict__ b) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+// lam_i = S_ii / G_ii; the diagonals themselves into dS, dG when given.
+__global__ void k_rayleigh(int N, const double *__restrict__ G, const double *__restrict__ S,
+                           double *__restrict__ lam, double *__restrict__ dS,
+                           double *__restrict__ dG) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double s = S[i + (size_t)i * N], g = G[i + (size_t)i * N];
+  lam[i] = s / g;
+  if (dS) {
+    dS[i] = s;
+    dG[i] = g;
+  }
+}
+
+// Rayleigh quotient of the updated column x'_j = X t_j (t_j = e_j + E e_j in the
+// rotated basis) to second order in E: x'^T M x' = t^T S t and x'^T x' = t^T G t with
+// the terms E_ij E_kj S_ik (i != k, third order) dropped; the -E E^T / 2 term of the
+// update changes the quotient only at third order. One block per column j.
+__global__ void k_eig_update(int N, const double *__restrict__ G, const double *__restrict__ S,
+                             const double *__restrict__ T, const double *__restrict__ dS,
+                             const double *__restrict__ dG, double *__restrict__ lam) {
+  __shared__ double rn[256], rd[256];
+  const int j = blockIdx.x;
+  const size_t c = (size_t)j * N;
+  double num = 0.0, den = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    if (i == j) continue;
+    const double e = T[c + i];
+    num += e * (2.0 * S[c + i] + e * dS[i]);
+    den += e * (2.0 * G[c + i] + e * dG[i]);
+  }
+  rn[threadIdx.x] = num;
+  rd[threadIdx.x] = den;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      rn[threadIdx.x] += rn[threadIdx.x + w];
+      rd[threadIdx.x] += rd[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ejj = T[c + j];
+    lam[j] = (dS[j] * (1.0 + 2.0 * ejj) + rn[0]) / (dG[j] * (1.0 + 2.0 * ejj) + rd[0]);
+  }
+}
+
+// colm[j] = max over i != j of |S_ij - (lam_i + lam_j) / 2 G_ij|, the largest
+// first-order coupling of column j (symmetric in i, j). One block per column.
+__global__ void k_col_coupling(int N, const double *__restrict__ G, const double *__restrict__ S,
+                               const double *__restrict__ lam, double *__restrict__ colm) {
+  __shared__ double red[256];
+  const int j = blockIdx.x;
+  const size_t c = (size_t)j * N;
+  const double lj = lam[j];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x)
+    if (i != j) m = fmax(m, fabs(S[c + i] - 0.5 * (lam[i] + lj) * G[c + i]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) colm[j] = red[0];
+}
+
+// Neighbours k, k+1 belong to one cluster when their Rayleigh quotients differ by
+// at most max(colm_k, colm_k+1) / kTau (the first-order update of that pair would
+// exceed kTau). cstart[k], csize[k]: the run around k. A run longer than
+// kMaxCluster sets bit 1 of *flag (the solve then falls back to dsyevd).
+__device__ __forceinline__ bool joined(const double *lam, const double *colm, int k) {
+  return fabs(lam[k + 1] - lam[k]) <= fmax(colm[k], colm[k + 1]) / kTau;
+}
+
+__global__ void k_clusters(int N, const double *__restrict__ lam, const double *__restrict__ colm,
+                           int *__restrict__ cstart, int *__restrict__ csize, int *flag) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int s = k;
+  while (s > 0 && k - s < kMaxCluster - 1 && joined(lam, colm, s - 1)) --s;
+  bool too_long = s > 0 && k - s == kMaxCluster - 1 && joined(lam, colm, s - 1);
+  int e = k + 1;
+  while (e < N && e - s < kMaxCluster && joined(lam, colm, e - 1)) ++e;
+  too_long = too_long || (e < N && e - s == kMaxCluster && joined(lam, colm, e - 1));
+  if (too_long) atomicOr(flag, 1);
+  cstart[k] = s;
+  csize[k] = e - s;
+}
+
+constexpr int kLd = kMaxCluster + 1;  // padded row of the shared blocks
+constexpr size_t kClusterSmem = 3 * (size_t)kMaxCluster * kLd * sizeof(double);
+constexpr size_t kBlkSmem = 2 * (size_t)kMaxCluster * kLd * sizeof(double);
+
+// One block of kMaxCluster threads per cluster of size >= 2 (block k where
+// cstart[k] == k): V_C with V_C^T G_CC V_C = I and V_C^T S_CC V_C diagonal, stored
+// as rows k..k+m-1 of Vbuf (N x kMaxCluster, row-major). Failures set bit 2 of *flag.
+__global__ void __launch_bounds__(kMaxCluster) k_cluster_eig(
+    int N, const double *__restrict__ G, const double *__restrict__ S, const int *__restrict__ cstart,
+    const int *__restrict__ csize, double *__restrict__ Vbuf, int *flag, int *maxc) {
+  const int k = blockIdx.x;
+  const int m = csize[k];
+  if (cstart[k] != k || m < 2) return;
+  extern __shared__ double sm[];
+  double *A = sm, *C = sm + kMaxCluster * kLd, *V = sm + 2 * kMaxCluster * kLd;
+  __shared__ double red[2][kMaxCluster];
+  const int l = threadIdx.x;
+  if (l < m)
+    for (int b = 0; b < m; ++b) {
+      size_t e = (size_t)(k + l) + (size_t)(k + b) * N;
+      A[l * kLd + b] = S[e];
+      C[l * kLd + b] = G[e];
+      V[l * kLd + b] = l == b ? 1.0 : 0.0;
+    }
+  __syncthreads();
+  // G_CC = C C^T (lower, left-looking)
+  for (int j = 0; j < m; ++j) {
+    if (l == 0) {
+      double d = C[j * kLd + j];
+      for (int q = 0; q < j; ++q) d -= C[j * kLd + q] * C[j * kLd + q];
+      C[j * kLd + j] = d > 0.0 ? sqrt(d) : -1.0;
+    }
+    __syncthreads();
+    const double cjj = C[j * kLd + j];
+    if (!(cjj > 0.0)) {
+      if (l == 0) atomicOr(flag, 2);
+      return;  // uniform: every thread read the same cjj
+    }
+    if (l > j && l < m) {
+      double v = C[l * kLd + j];
+      for (int q = 0; q < j; ++q) v -= C[l * kLd + q] * C[j * kLd + q];
+      C[l * kLd + j] = v / cjj;
+    }
+    __syncthreads();
+  }
+  // A <- C^-1 A (thread = column), then A <- A C^-T (thread = row), symmetrise
+  if (l < m)
+    for (int i = 0; i < m; ++i) {
+      double v = A[i * kLd + l];
+      for (int q = 0; q < i; ++q) v -= C[i * kLd + q] * A[q * kLd + l];
+      A[i * kLd + l] = v / C[i * kLd + i];
+    }
+  __syncthreads();
+  if (l < m)
+    for (int b = 0; b < m; ++b) {
+      double v = A[l * kLd + b];
+      for (int q = 0; q < b; ++q) v -= A[l * kLd + q] * C[b * kLd + q];
+      A[l * kLd + b] = v / C[b * kLd + b];
+    }
+  __syncthreads();
+  if (l < m)
+    for (int b = l + 1; b < m; ++b) {
+      double v = 0.5 * (A[l * kLd + b] + A[b * kLd + l]);
+      A[l * kLd + b] = v;
+      A[b * kLd + l] = v;
+    }
+  __syncthreads();
+  // cyclic Jacobi (Golub and Van Loan, Alg. 8.5.3), at most 40 sweeps
+  bool converged = false;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    if (l < m)
+      for (int b = 0; b < m; ++b) {
+        double v = A[l * kLd + b] * A[l * kLd + b];
+        tot += v;
+        if (b != l) off += v;
+      }
+    red[0][l] = off;
+    red[1][l] = tot;
+    __syncthreads();
+    for (int w = kMaxCluster / 2; w > 0; w >>= 1) {
+      if (l < w) {
+        red[0][l] += red[0][l + w];
+        red[1][l] += red[1][l + w];
+      }
+      __syncthreads();
+    }
+    converged = red[0][0] <= 1e-30 * red[1][0];
+    __syncthreads();
+    if (converged) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = A[p * kLd + q];
+        if (apq == 0.0) continue;  // uniform: all threads read the same value
+        const double theta = (A[q * kLd + q] - A[p * kLd + p]) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        __syncthreads();
+        if (l < m) {
+          double aip = A[l * kLd + p], aiq = A[l * kLd + q];
+          A[l * kLd + p] = c * aip - sn * aiq;
+          A[l * kLd + q] = sn * aip + c * aiq;
+        }
+        __syncthreads();
+        if (l < m) {
+          double api = A[p * kLd + l], aqi = A[q * kLd + l];
+          A[p * kLd + l] = c * api - sn * aqi;
+          A[q * kLd + l] = sn * api + c * aqi;
+          double vip = V[l * kLd + p], viq = V[l * kLd + q];
+          V[l * kLd + p] = c * vip - sn * viq;
+          V[l * kLd + q] = sn * vip + c * viq;
+        }
+        __syncthreads();
+      }
+  }
+  if (!converged) {
+    if (l == 0) atomicOr(flag, 2);
+    return;
+  }
+  // Order the block's eigenpairs by eigenvalue (Jacobi leaves them unordered): the
+  // next iteration groups clusters from neighbouring indices, which must then hold
+  // neighbouring eigenvalues.
+  __shared__ int perm[kMaxCluster];
+  if (l == 0) {
+    for (int b = 0; b < m; ++b) perm[b] = b;
+    for (int b = 1; b < m; ++b) {  // insertion sort on the diagonal of A
+      const int pb = perm[b];
+      const double v = A[pb * kLd + pb];
+      int q = b - 1;
+      while (q >= 0 && A[perm[q] * kLd + perm[q]] > v) {
+        perm[q + 1] = perm[q];
+        --q;
+      }
+      perm[q + 1] = pb;
+    }
+  }
+  __syncthreads();
+  if (l < m)
+    for (int b = 0; b < m; ++b) A[l * kLd + b] = V[l * kLd + perm[b]];
+  __syncthreads();
+  if (l < m)
+    for (int b = 0; b < m; ++b) V[l * kLd + b] = A[l * kLd + b];
+  __syncthreads();
+  // V_C = C^-T V (thread = column, backward substitution)
+  if (l < m)
+    for (int i = m - 1; i >= 0; --i) {
+      double v = V[i * kLd + l];
+      for (int q = i + 1; q < m; ++q) v -= C[q * kLd + i] * V[q * kLd + l];
+      V[i * kLd + l] = v / C[i * kLd + i];
+    }
+  __syncthreads();
+  if (l < m)
+    for (int b = 0; b < m; ++b) Vbuf[(size_t)(k + l) * kMaxCluster + b] = V[l * kLd + b];
+  if (l == 0) atomicMax(maxc, m);
+}
+
+// X[:, C] <- X[:, C] V_C for every cluster C, rows 0..nrows-1 (kMaxCluster rows
+// per block; the block of X and V_C staged in shared memory).
+__global__ void __launch_bounds__(kMaxCluster) k_blk_right(
+    int nrows, double *__restrict__ X, long long ld, const int *__restrict__ cstart,
+    const int *__restrict__ csize, const double *__restrict__ Vbuf) {
+  const int k = blockIdx.y;
+  const int m = csize[k];
+  if (cstart[k] != k || m < 2) return;
+  extern __shared__ double sm[];
+  double *Vs = sm, *Xs = sm + kMaxCluster * kLd;
+  const int t = threadIdx.x;
+  for (int b = 0; b < m; ++b)
+    if (t < m) Vs[b * kLd + t] = Vbuf[(size_t)(k + b) * kMaxCluster + t];
+  const int i = blockIdx.x * kMaxCluster + t;
+  if (i < nrows)
+    for (int b = 0; b < m; ++b) Xs[t * kLd + b] = X[i + (size_t)(k + b) * ld];
+  __syncthreads();
+  if (i >= nrows) return;
+  for (int j = 0; j < m; ++j) {
+    double v = 0.0;
+    for (int b = 0; b < m; ++b) v += Xs[t * kLd + b] * Vs[b * kLd + j];
+    X[i + (size_t)(k + j) * ld] = v;
+  }
+}
+
+// X[C, :] <- V_C^T X[C, :] (trans = 1) or V_C X[C, :] (trans = 0), columns 0..ncols-1.
+__global__ void __launch_bounds__(kMaxCluster) k_blk_left(
+    int ncols, double *__restrict__ X, long long ld, int trans, const int *__restrict__ cstart,
+    const int *__restrict__ csize, const double *__restrict__ Vbuf) {
+  const int k = blockIdx.y;
+  const int m = csize[k];
+  if (cstart[k] != k || m < 2) return;
+  extern __shared__ double sm[];
+  double *Vs = sm, *Xs = sm + kMaxCluster * kLd;
+  const int t = threadIdx.x;
+  // Vs[a][b] = (trans ? V^T : V)[a][b]
+  for (int a = 0; a < m; ++a)
+    if (t < m)
+      Vs[a * kLd + t] = trans ? Vbuf[(size_t)(k + t) * kMaxCluster + a]
+                              : Vbuf[(size_t)(k + a) * kMaxCluster + t];
+  const int c = blockIdx.x * kMaxCluster + t;
+  if (c < ncols)
+    for (int b = 0; b < m; ++b) Xs[t * kLd + b] = X[(size_t)(k + b) + (size_t)c * ld];
+  __syncthreads();
+  if (c >= ncols) return;
+  for (int a = 0; a < m; ++a) {
+    double v = 0.0;
+    for (int b = 0; b < m; ++b) v += Vs[a * kLd + b] * Xs[t * kLd + b];
+    X[(size_t)(k + a) + (size_t)c * ld] = v;
+  }
+}
+
+// E from the rotated G, S and their Rayleigh quotients. Below the diagonal
+// E_ij = (S_ij - lam_j G_ij) / (lam_j - lam_i); above it E_ij = -G_ij - E_ji, so that
+// (I + E)^T G (I + E) = I holds to first order whatever rounding made S slightly
+// unsymmetric (for nearly equal lam that rounding, divided by the gap, then turns
+// the pair instead of tilting it). Inside a cluster E = (I - G) / 2. A cross-cluster
+// |E| above 1/2 (first order no longer valid) sets bit 4 of *flag.
+__global__ void k_form_update(int N, const double *__restrict__ G, const double *__restrict__ S,
+                              const double *__restrict__ lam, const int *__restrict__ cstart,
+                              double *__restrict__ E, int *flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= N) return;
+  const size_t e = i + (size_t)j * N;
+  double t;
+  if (cstart[i] == cstart[j]) {
+    t = 0.5 * ((i == j ? 1.0 : 0.0) - G[e]);
+  } else {
+    const int r = i > j ? i : j, c = i > j ? j : i;  // lower-triangle element (r, c)
+    const size_t el = r + (size_t)c * N;
+    const double elow = (S[el] - lam[c] * G[el]) / (lam[c] - lam[r]);
+    if (!(fabs(elow) <= 0.5)) atomicOr(flag, 4);
+    t = i > j ? elow : -G[e] - elow;
+    if (!(fabs(t) <= 1.0)) t = 0.0;
+  }
+  E[e] = t;
+}
+
+// T = I + E - D / 2 with D = E E^T: the second-order term that keeps X (I + E)
+// orthonormal to third order (E is antisymmetric to first order, so E E^T stands
+// in for E^T E). In place over E.
+__global__ void k_second_order(size_t NN, int N, double *__restrict__ E,
+                               const double *__restrict__ D) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < NN;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t j = e / N, i = e - j * N;
+    E[e] = (i == j ? 1.0 : 0.0) + E[e] - 0.5 * D[e];
+  }
+}
+
+// Normalise every column of X to unit length (one block per column).
+__global__ void k_colnorm(int N, double *__restrict__ X) {
+  __shared__ double red[256];
+  double *x = X + (size_t)blockIdx.x * N;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) s += x[i] * x[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double f = red[0] > 0.0 ? 1.0 / sqrt(red[0]) : 0.0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) x[i] *= f;
+}
+
+// C (m x n, ldc = m) = op(A) B with op(A) = A (transA = 0, A m x k) or A^T (A k x m),
+// B k x n, all leading dimensions equal to the row count N of the square case.
+int product(gc_context *ctx, int prec, bool transA, int m, int n, int k, const double *A,
+            int lda, const double *B, int ldb, double *C, int ldc) {
+  if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6)
+    return gc::tc_gemm_strided(ctx, prec, m, n, k, A, transA ? lda : 1, transA ? 1 : lda, B, ldb,
+                               1, C, ldc);
+  const double one = 1.0, zero = 0.0;
+  GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, transA ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, m, n, k,
+                             &one, A, lda, B, ldb, &zero, C, ldc));
+  return GC_OK;
+}
+
+// FP32 eigensolve of M plus ctx->eig_refine refinement iterations. On success
+// Xout (N x N) holds the eigenvectors, lam (N) the eigenvalues (the second-order
+// Rayleigh quotients of the updated vectors), *fallback = false.
+// *fallback = true when the FP32 solver failed or a cluster could not be handled.
+int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout, double *lam,
+                bool *fallback) {
+  *fallback = false;
+  const size_t NN = (size_t)N * N;
+  gc::DevBuf<float> m32, w32, work;
+  gc::DevBuf<double> U0, U1, vbuf, dS, dG;
+  gc::DevBuf<int> cst, csz, flag;
+  gc::DevBuf<double> colm;
+  GC_TRY(m32.alloc(ctx, NN));
+  GC_TRY(w32.alloc(ctx, N));
+  GC_TRY(U0.alloc(ctx, 2 * NN));
+  GC_TRY(U1.alloc(ctx, 2 * NN));
+  GC_TRY(vbuf.alloc(ctx, (size_t)N * kMaxCluster));
+  GC_TRY(dS.alloc(ctx, N));
+  GC_TRY(dG.alloc(ctx, N));
+  GC_TRY(cst.alloc(ctx, N));
+  GC_TRY(csz.alloc(ctx, N));
+  GC_TRY(flag.alloc(ctx, 2));
+  GC_TRY(colm.alloc(ctx, N));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_cluster_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kClusterSmem));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_right, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kBlkSmem));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_left, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kBlkSmem));
+  GC_CUDA(ctx, cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), ctx->stream));
+  const unsigned ew = std::min<size_t>(gc::ceil_div(NN, 256), 152 * 16);
+  k_d2f<<<ew, 256, 0, ctx->stream>>>(NN, M, m32.p);
+  GC_LAUNCHED(ctx);
+  {
+    int lwork = 0;
+    GC_CUSOLVER(ctx, cusolverDnSsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR,
+                                                 CUBLAS_FILL_MODE_LOWER, N, m32.p, N, w32.p, &lwork));
+    GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
+    if (ctx->eig_emulation)
+      GC_CUSOLVER(ctx, cusolverDnSetMathMode(ctx->cusolver, CUSOLVER_FP32_EMULATED_BF16X9_MATH));
+    cusolverStatus_t st = cusolverDnSsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR,
+                                           CUBLAS_FILL_MODE_LOWER, N, m32.p, N, w32.p, work.p, lwork,
+                                           ctx->dev_info);
+    if (ctx->eig_emulation)
+      GC_CUSOLVER(ctx, cusolverDnSetMathMode(ctx->cusolver, CUSOLVER_DEFAULT_MATH));
+    GC_CUSOLVER(ctx, st);
+    work.release();
+    int info = 0;
+    GC_CUDA(ctx, cudaMemcpyAsync(&info, ctx->dev_info, sizeof(int), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (info != 0) {
+      *fallback = true;
+      return GC_OK;
+    }
+  }
+  k_f2d<<<ew, 256, 0, ctx->stream>>>(NN, m32.p, U0.p);
+  GC_LAUNCHED(ctx);
+  m32.release();
+  double *cur = U0.p, *nxt = U1.p;
+  const int iters = std::max(1, std::min(4, ctx->eig_refine));
+  const unsigned gN = gc::ceil_div(N, 256);
+  const dim3 b2(32, 8), g2(gc::ceil_div(N, 32), gc::ceil_div(N, 8));
+  for (int it = 0; it < iters; ++it) {
+    double *X = cur, *P = cur + NN, *G = nxt, *S = nxt + NN;
+    GC_TRY(product(ctx, prec, false, N, N, N, M, N, X, N, P, N));        // P = M X
+    GC_TRY(product(ctx, prec, true, N, 2 * N, N, X, N, X, N, G, N));     // [G S] = X^T [X P]
+    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, G);
+    GC_LAUNCHED(ctx);
+    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, S);
+    GC_LAUNCHED(ctx);
+    k_rayleigh<<<gN, 256, 0, ctx->stream>>>(N, G, S, lam, nullptr, nullptr);
+    GC_LAUNCHED(ctx);
+    k_col_coupling<<<N, 256, 0, ctx->stream>>>(N, G, S, lam, colm.p);
+    GC_LAUNCHED(ctx);
+    k_clusters<<<gN, 256, 0, ctx->stream>>>(N, lam, colm.p, cst.p, csz.p, flag.p);
+    GC_LAUNCHED(ctx);
+    k_cluster_eig<<<N, kMaxCluster, kClusterSmem, ctx->stream>>>(N, G, S, cst.p, csz.p, vbuf.p,
+                                                                 flag.p, flag.p + 1);
+    GC_LAUNCHED(ctx);
+    const dim3 gr(gc::ceil_div(N, kMaxCluster), N), gl2(gc::ceil_div(2 * (size_t)N, kMaxCluster), N);
+    k_blk_right<<<gr, kMaxCluster, kBlkSmem, ctx->stream>>>(N, G, N, cst.p, csz.p, vbuf.p);
+    GC_LAUNCHED(ctx);
+    k_blk_right<<<gr, kMaxCluster, kBlkSmem, ctx->stream>>>(N, S, N, cst.p, csz.p, vbuf.p);
+    GC_LAUNCHED(ctx);
+    k_blk_left<<<gl2, kMaxCluster, kBlkSmem, ctx->stream>>>(2 * N, G, N, 1, cst.p, csz.p, vbuf.p);
+    GC_LAUNCHED(ctx);
+    k_rayleigh<<<gN, 256, 0, ctx->stream>>>(N, G, S, lam, dS.p, dG.p);
+    GC_LAUNCHED(ctx);
+    k_form_update<<<dim3(gN, N), 256, 0, ctx->stream>>>(N, G, S, lam, cst.p, P, flag.p);
+    GC_LAUNCHED(ctx);
+    k_eig_update<<<N, 256, 0, ctx->stream>>>(N, G, S, P, dS.p, dG.p, lam);
+    GC_LAUNCHED(ctx);
+    // D = E E^T into the S slot (S is no longer needed); low relative accuracy suffices
+    if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6) {
+      GC_TRY(gc::tc_gemm_nt(ctx, GC_PREC_BF16X6, N, N, N, P, N, P, N, S, N));
+    } else {
+      const double one = 1.0, zero = 0.0;
+      GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, N, N, N, &one, P, N, P, N,
+                                 &zero, S, N));
+    }
+    k_second_order<<<ew, 256, 0, ctx->stream>>>(NN, N, P, S);
+    GC_LAUNCHED(ctx);
+    k_blk_left<<<gr, kMaxCluster, kBlkSmem, ctx->stream>>>(N, P, N, 0, cst.p, csz.p, vbuf.p);
+    GC_LAUNCHED(ctx);
+    GC_TRY(product(ctx, prec, false, N, N, N, X, N, P, N, G, N));        // X' = X (V (I + E))
+    std::swap(cur, nxt);
+  }
+  int hflag[2] = {0, 0};
+  GC_CUDA(ctx, cudaMemcpyAsync(hflag, flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->refine_max_cluster = std::max(ctx->refine_max_cluster, hflag[1]);
+  if (hflag[0] != 0) {
+    *fallback = true;
+    return GC_OK;
+  }
+  k_colnorm<<<N, 256, 0, ctx->stream>>>(N, cur);
+  GC_LAUNCHED(ctx);
+  GC_CUDA(ctx, cudaMemcpyAsync(Xout, cur, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  return GC_OK;
+}
+
+// Eigenpairs of the symmetric M in place (vectors overwrite M, values in w):
+// dsyevd, or the refined FP32 solve with dsyevd as its fallback.
+int eigen(gc_context *ctx, int N, double *M, double *w, int mode, int prec) {
+  if (mode != GC_ERPA_CHOLESKY_REFINED) return syevd(ctx, N, M, w);
+  ctx->refine_solves++;
+  bool fallback = N > 65535;
+  if (!fallback) GC_TRY(refined_eig(ctx, N, prec, M, M, w, &fallback));
+  if (fallback) {
+    ctx->refine_fallbacks++;
+    return syevd(ctx, N, M, w);
+  }
+  return GC_OK;
+}
+
 }  // namespace
 
 namespace gc {
@@ -150,7 +692,7 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_LAUNCHED(ctx);
     return GC_OK;
   }
-  if (mode == GC_ERPA_CHOLESKY) {
+  if (mode == GC_ERPA_CHOLESKY || mode == GC_ERPA_CHOLESKY_REFINED) {
     DevBuf<double> L, M;
     GC_TRY(L.alloc(ctx, NN));
     GC_TRY(M.alloc(ctx, NN));
@@ -182,7 +724,7 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
       GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, N, 1, Y, N, 1, M.p, N));
       k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
       GC_LAUNCHED(ctx);
-      GC_TRY(syevd(ctx, N, M.p, eig));
+      GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
       GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, 1, N, M.p, N, 1, Y, N));
     } else {
       // M = A- L (into Y as scratch), then M = L^T (A- L)
@@ -190,7 +732,11 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
                                  CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N, Y, N));
       GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
                                  CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N, M.p, N));
-      GC_TRY(syevd(ctx, N, M.p, eig));
+      if (mode == GC_ERPA_CHOLESKY_REFINED) {
+        k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
+        GC_LAUNCHED(ctx);
+      }
+      GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
       // Y = L U
       GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
                                  CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, M.p, N, Y, N));
@@ -210,4 +756,29 @@ extern "C" int gc_erpa(gc_context *ctx, int ndimx, double *abplus, double *abmin
                        double *eig, int mode) {
   if (!ctx) return GC_EINVAL;
   return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, GC_PREC_FP64);
+}
+
+extern "C" int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus, double *abmin,
+                          double *eigvec, double *eig, int mode, int precision) {
+  if (!ctx) return GC_EINVAL;
+  if (precision != GC_PREC_FP64 && precision != GC_PREC_FP64TC5 && precision != GC_PREC_FP64TC6)
+    return gc::set_error(ctx, GC_EINVAL, "gc_erpa_ex: precision %d is not FP64-accurate", precision);
+  return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, precision);
+}
+
+extern "C" int gc_set_eig_refinement(gc_context *ctx, int iterations) {
+  if (!ctx) return GC_EINVAL;
+  if (iterations < 1 || iterations > 4)
+    return gc::set_error(ctx, GC_EINVAL, "refinement iterations %d outside 1..4", iterations);
+  ctx->eig_refine = iterations;
+  return GC_OK;
+}
+
+extern "C" int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,
+                                   int *max_cluster) {
+  if (!ctx) return GC_EINVAL;
+  if (solves) *solves = ctx->refine_solves;
+  if (fallbacks) *fallbacks = ctx->refine_fallbacks;
+  if (max_cluster) *max_cluster = ctx->refine_max_cluster;
+  return GC_OK;
 }

@@ -22,6 +22,10 @@ struct gc_context {
   int *dev_flag = nullptr;           // device error flag for bounded waits
   long long launches = 0;            // kernels of this library launched
   int eig_emulation = 0;             // cuSOLVER FP64 emulation strategy EAGER when 1
+  int eig_refine = 2;                // refinement iterations of the FP32 eigensolve
+  long long refine_solves = 0;       // GC_ERPA_CHOLESKY_REFINED solves
+  long long refine_fallbacks = 0;    // of which fell back to dsyevd
+  int refine_max_cluster = 0;        // largest cluster diagonalised in a block
   std::string err;
 };
 

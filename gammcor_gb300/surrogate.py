@@ -10,7 +10,8 @@ and the sizes of the system. That is 2 ERPA solves per energy instead of 8.
 An ensemble of networks supplies the error estimate: three times the spread of
 the members' energies. When the estimate is above the requested threshold the
 energy falls back to the full 8-point quadrature, which reuses the two end-node
-solves, so a fallback costs the same as not using the surrogate at all.
+solves and the system's integrals and A+-B (kept on the device by a batch
+session), so a fallback costs the exact quadrature plus the network.
 
 Training data come from the exact path (FP64-accurate; it agrees with the plain
 FP64 GPU path to ~1e-9 Eh). The networks are trained and evaluated by this
@@ -177,29 +178,31 @@ MODEL = __import__("pathlib").Path(__file__).resolve().parent / "data" / "surrog
 
 
 def energies(batch, ens: Ensemble, threshold: float = 1e-6, nstreams: int = 8,
-             precision: str = "fp64tc5", eig_emulation: bool = False):
+             precision: str = "fp64tc5", eig_emulation: bool = False,
+             erpa_mode: str = "refined", eig_refine: int = 0):
     """AC-CAS energies of a batch with the surrogate: ERPA at the two end nodes
     for every system, the ensemble's prediction where its error estimate is at
-    most `threshold`, and the six interior nodes (reusing the end nodes) where
-    it is not. Returns (energies, fallback mask, estimate, status)."""
+    most `threshold`, and the six interior nodes where it is not. One session
+    holds every system's integrals and A+-B between the two passes, so a
+    rejected system costs the exact 8-point quadrature plus the network.
+    Returns (energies, fallback mask, estimate, status)."""
     x8, w8 = gauss8()
-    ends = list(END)
-    kw = dict(nstreams=nstreams, precision=precision, eig_emulation=eig_emulation)
-    ea, _, wa, st, om = api.ac_energy_batched(batch, lambdas=x8[ends], weights=w8[ends],
-                                              omega_stats=True, **kw)
-    nd = batch.ndimx()
-    X = np.array([features(s, wa[i], om[i], nd[i]) for i, s in enumerate(batch.systems)])
-    e_pred, e_est = estimate(ens, X, wa, w8)
-    fb = ~(e_est <= threshold) | (st != 0)
-    e = e_pred.copy()
-    if fb.any():
-        idx = np.nonzero(fb)[0]
-        inner = list(INNER)
-        eb, _, _, stb = api.ac_energy_batched(batch.subset(idx), lambdas=x8[inner],
-                                              weights=w8[inner], **kw)
-        e[idx] = ea[idx] + eb
+    ends, inner = list(END), list(INNER)
+    with api.AcSession(batch, precision=precision, erpa_mode=erpa_mode, nstreams=nstreams,
+                       eig_emulation=eig_emulation, eig_refine=eig_refine) as ses:
+        allidx = np.arange(len(batch.systems))
+        wa, _, st, om = ses.points(allidx, x8[ends], omega_stats=True)
+        nd = batch.ndimx()
+        X = np.array([features(s, wa[i], om[i], nd[i]) for i, s in enumerate(batch.systems)])
+        e_pred, e_est = estimate(ens, X, wa, w8)
+        fb = ~(e_est <= threshold) | (st != 0)
+        e = e_pred.copy()
         st = st.copy()
-        st[idx] = np.maximum(st[idx], stb)
+        if fb.any():
+            idx = np.nonzero(fb)[0]
+            wb, _, stb = ses.points(idx, x8[inner])
+            e[idx] = wa[idx] @ w8[ends] + wb @ w8[inner]
+            st[idx] = np.maximum(st[idx], stb)
     return e, fb, e_est, st
 
 

@@ -47,7 +47,14 @@ enum gc_precision {
 /* ERPA eigen-solver form. */
 enum gc_erpa_mode {
   GC_ERPA_SYMM1 = 0,     /* ERPASYMM1: eig(A+), A+^1/2 A- A+^1/2, eig  (2 eigensolves) */
-  GC_ERPA_CHOLESKY = 1   /* A+ = L L^T, eig(L^T A- L), Y = L u / sqrt(2 w) (1 eigensolve) */
+  GC_ERPA_CHOLESKY = 1,  /* A+ = L L^T, eig(L^T A- L), Y = L u / sqrt(2 w) (1 eigensolve) */
+  GC_ERPA_CHOLESKY_REFINED = 2 /* as GC_ERPA_CHOLESKY, with the eigensolve of L^T A- L done in
+                          FP32 (ssyevd) and refined to FP64 accuracy: per iteration the Rayleigh
+                          matrices S = X^T M X and G = X^T X in the GEMM precision, clusters of
+                          close eigenvalues diagonalised exactly in FP64, and the update
+                          X <- X (I + E - E E^T / 2) with E first order in the residual for the
+                          rest. Falls back to dsyevd when a cluster is wider than 64 or a block
+                          is singular */
 };
 
 /* Context ------------------------------------------------------------- */
@@ -60,8 +67,16 @@ int gc_synchronize(gc_context *ctx);
 long long gc_kernel_launches(const gc_context *ctx);
 /* on = 1 lets cuSOLVER run the FP64 eigensolver's internal matrix products with
  * its fixed-point FP64 emulation on tensor cores (cusolverDnSetEmulationStrategy
- * EAGER); on = 0 restores the default. The eigensolver stays an FP64 dsyevd. */
+ * EAGER), and the FP32 eigensolver of GC_ERPA_CHOLESKY_REFINED with BF16x9
+ * emulated FP32 math (CUSOLVER_FP32_EMULATED_BF16X9_MATH); on = 0 restores the
+ * defaults. */
 int gc_set_eig_emulation(gc_context *ctx, int on);
+/* Refinement iterations of GC_ERPA_CHOLESKY_REFINED (default 2, range 1..4). */
+int gc_set_eig_refinement(gc_context *ctx, int iterations);
+/* Counters of GC_ERPA_CHOLESKY_REFINED on a context: solves, solves that fell back to
+ * dsyevd, and the largest cluster of close eigenvalues diagonalised in a block. */
+int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,
+                        int *max_cluster);
 
 /* Host-side helpers ----------------------------------------------------- */
 
@@ -121,6 +136,12 @@ int gc_ab_cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
  * ascending. */
 int gc_erpa(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
             double *eigvec_dev, double *eig_dev, int mode);
+/* gc_erpa with the arithmetic of the Cholesky form's matrix products (and of the
+ * refinement products of GC_ERPA_CHOLESKY_REFINED) chosen by precision: GC_PREC_FP64
+ * (cuBLAS) or GC_PREC_FP64TC5 / GC_PREC_FP64TC6 (sliced tensor-core GEMM). The
+ * eigenvalues of the refined mode are not sorted. */
+int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
+               double *eigvec_dev, double *eig_dev, int mode, int precision);
 
 /* Integrand ---------------------------------------------------------------- */
 
@@ -185,6 +206,7 @@ typedef struct gc_ac_params {
   int affine;      /* 1: assemble A+-B at lambda = 0 and 1 once, combine per point */
   int nstreams;    /* concurrent worker streams */
   int eig_emulation; /* 1: gc_set_eig_emulation on every worker context */
+  int eig_refine;  /* refinement iterations of GC_ERPA_CHOLESKY_REFINED (0: default 2) */
   const double *lambda;  /* host, ngrid points; NULL: Gauss-Legendre points on [0,1] */
   const double *weight;  /* host, ngrid weights used with lambda (NULL: all zero) */
 } gc_ac_params;
@@ -202,6 +224,26 @@ typedef struct gc_ac_params {
 int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *sys,
                          const gc_ac_params *par, double *ecorr, double *ecas,
                          double *w_lambda, double *omega_stats, int *status);
+
+/* A batch whose per-system device state (FFOO, FOFO, A+-B at lambda = 0 and 1)
+ * stays resident between calls, so that lambda points can be added to some of
+ * its systems later without repeating the transform or the assembly (the
+ * integrand surrogate evaluates the end nodes of every system first and the
+ * interior nodes only where its error estimate rejects the prediction). The
+ * state of a system is built on its first use. par->affine must be 1; ngrid,
+ * lambda and weight of par are not used. sys and the host arrays it points to
+ * must stay valid until gc_ac_session_destroy. */
+typedef struct gc_ac_session gc_ac_session;
+int gc_ac_session_create(gc_context *ctx, int nsys, const gc_system *sys,
+                         const gc_ac_params *par, gc_ac_session **session);
+/* W(lambda) at npoints points (host lambda) for the systems idx[0..nidx) (distinct
+ * indices into the session's systems): w_out (nidx*npoints), omega_stats
+ * (nidx*npoints*GC_OMEGA_STATS, may be NULL), ecas (nidx, may be NULL), status
+ * (nidx, may be NULL; as in gc_ac_energy_batched). Outputs follow the order of idx. */
+int gc_ac_session_points(gc_ac_session *session, int nidx, const int *idx, int npoints,
+                         const double *lambda, double *w_out, double *omega_stats,
+                         double *ecas, int *status);
+int gc_ac_session_destroy(gc_ac_session *session);
 
 /* Integrand surrogate (no counterpart in the reference) ---------------------
  * Multilayer perceptron in -> H -> H -> H -> out with GELU on the hidden layers,

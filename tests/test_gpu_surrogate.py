@@ -16,3 +16,51 @@ def test_surrogate_beats_the_method_without_it(gpu_lib):
     ens.fit(tr["X"], surrogate.targets(tr["W"]), epochs=1500, log=quiet)
     res = surrogate.evaluate(ens, te, thresholds=(1e-3,))
     assert res["mae_network"] < res["mae_without_network"], res
+
+
+def test_gated_energies_equal_the_exact_quadrature(gpu_lib):
+    """surrogate.energies with the threshold at zero rejects every prediction: the
+    end-node pass plus the interior pass of the batch session must then give the
+    8-point energies of the one-call batch."""
+    import numpy as np
+    from gammcor_gb300 import api, synth
+    shapes = surrogate.shapes(5, seed=9, nmin=30, nmax=50)
+    systems = [synth.make_system_device(d["n"], d["nin"], d["nact"], d["rank"], d["seed"])
+               for d in shapes]
+    batch = api.BatchInputs(systems, "cuda:0")
+    ens = surrogate.Ensemble.load(surrogate.MODEL)
+    e, fb, est, st = surrogate.energies(batch, ens, threshold=0.0, nstreams=3)
+    assert fb.all() and (st == 0).all()
+    ref = api.ac_energy_batched(batch, ngrid=8, precision="fp64tc5", erpa_mode="refined",
+                                nstreams=3)[0]
+    np.testing.assert_allclose(e, ref, atol=1e-10, rtol=0)
+
+
+def test_session_points_reuse_state_and_validate(gpu_lib):
+    import numpy as np
+    from gammcor_gb300 import api, synth
+    from gammcor_gb300._lib import GcError
+    shapes = surrogate.shapes(8, seed=10, nmin=30, nmax=50)
+    systems = [synth.make_system_device(d["n"], d["nin"], d["nact"], d["rank"], d["seed"])
+               for d in shapes]
+    # keep systems whose A+B is positive definite on all eight points
+    full = api.ac_energy_batched(api.BatchInputs(systems, "cuda:0"), ngrid=8,
+                                 precision="fp64tc5", erpa_mode="refined", nstreams=2)
+    systems = [s for s, st in zip(systems, full[3]) if st == 0][:4]
+    assert len(systems) == 4
+    batch = api.BatchInputs(systems, "cuda:0")
+    x8, w8 = surrogate.gauss8()
+    with api.AcSession(batch, nstreams=2) as ses:
+        w1, ecas1, st1 = ses.points([2, 0], x8[:3])
+        w2, ecas2, st2 = ses.points([0, 1, 2, 3], x8)
+        assert (st1 == 0).all() and (st2 == 0).all()
+        np.testing.assert_allclose(w2[[2, 0], :3], w1, atol=1e-12, rtol=0)
+        np.testing.assert_allclose(ecas2[[2, 0]], ecas1, atol=1e-12, rtol=0)
+        ref = api.ac_energy_batched(batch, ngrid=8, precision="fp64tc5", erpa_mode="refined",
+                                    nstreams=2)
+        np.testing.assert_allclose(w2 @ w8, ref[0], atol=1e-10, rtol=0)
+        np.testing.assert_allclose(ecas2, ref[1], atol=1e-10, rtol=0)
+        with pytest.raises(GcError):
+            ses.points([1, 1], x8[:1])
+        with pytest.raises(GcError):
+            ses.points([4], x8[:1])
