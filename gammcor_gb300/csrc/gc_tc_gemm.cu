@@ -111,6 +111,18 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
   return d;
 }
 
+// As smem_desc for 64-byte rows (32 BF16 of K) in the 64-byte swizzle: 8-row groups
+// 512 bytes apart, layout SWIZZLE_64B (bits 61-63 = 4).
+__device__ __forceinline__ uint64_t smem_desc64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;           // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;  // SBO
+  d |= (uint64_t)1 << 46;           // descriptor version
+  d |= (uint64_t)4 << 61;           // SWIZZLE_64B
+  return d;
+}
+
 // Instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, M=128, N=bn.
 __host__ __device__ constexpr uint32_t instr_desc(int bn) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) |
@@ -145,6 +157,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 lanes x 8 columns of 32-bit TMEM words, issued without waiting (several loads
+// can be in flight before one tmem_ld_wait()).
+__device__ __forceinline__ void tmem_ld8_issue(uint32_t taddr, uint32_t *r) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // ------------------------------------------------------------------- kernel
@@ -291,13 +316,16 @@ __global__ void __launch_bounds__(192, 1)
 // chunks short enough that every FP32 partial sum is an integer below 2^24, so
 // each chunk is exact, and the epilogue adds the chunks in FP64 registers.
 constexpr int OZ_BN = 64;
-constexpr int OZ_STAGES = 6;
+constexpr int OZ_BK = 32;      // K per stage: 32 BF16 = one 64-byte swizzled row
+constexpr int OZ_STAGES = 3;   // each stage holds every slice of A and of B
 constexpr int OZ_MAXS = 6;
+constexpr int OZ_EPI_WARPS = 8;                   // two per TMEM lane quarter
+constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;  // TMA warp, MMA warp, epilogue
 
 struct OzPlan {
   int S;          // slices per operand
   int npass;      // S(S+1)/2
-  int chunk_kb;   // 64-wide K blocks per exact chunk
+  int chunk_kb;   // OZ_BK-wide K blocks per exact chunk
   int pa[OZ_MAXS * (OZ_MAXS + 1) / 2], pb[OZ_MAXS * (OZ_MAXS + 1) / 2],
       pd[OZ_MAXS * (OZ_MAXS + 1) / 2];
 };
@@ -314,22 +342,24 @@ struct OzEpi {
 };
 
 template <int S>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(OZ_THREADS, 1)
     k_tc_gemm_oz(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  int M, int N, int kblocks, int a_batched, int b_batched, OzPlan plan, OzEpi epi,
                  int *err_flag) {
+  // One stage = the K block [kb*32, kb*32+32) of all S slices of the A tile (128 rows)
+  // and of the B tile (OZ_BN rows): every slice product t+u < S of the block is
+  // issued from it, so each slice tile crosses L2 -> shared memory once per block.
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = OZ_BN * BK * 2;
-  uint8_t *sA = smem;
-  uint8_t *sB = smem + OZ_STAGES * A_BYTES;
-  uint64_t *full = (uint64_t *)(sB + OZ_STAGES * B_BYTES);
+  constexpr uint32_t A_BYTES = BM * OZ_BK * 2, B_BYTES = OZ_BN * OZ_BK * 2;
+  constexpr uint32_t STAGE_BYTES = S * (A_BYTES + B_BYTES);
+  uint64_t *full = (uint64_t *)(smem + OZ_STAGES * STAGE_BYTES);
   uint64_t *empty = full + OZ_STAGES;
   uint64_t *accf = empty + OZ_STAGES;
   uint64_t *acce = accf + 1;
   uint32_t *tmem_slot = (uint32_t *)(acce + 1);
   __shared__ int abort_flag;
-  __shared__ double red[4];
+  __shared__ double red[OZ_EPI_WARPS];
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * OZ_BN, b = blockIdx.z;
@@ -341,7 +371,7 @@ __global__ void __launch_bounds__(192, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(accf, 1);
-    mbar_init(acce, 4);
+    mbar_init(acce, OZ_EPI_WARPS);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -357,28 +387,29 @@ __global__ void __launch_bounds__(192, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    int it = 0, issued = 0;
-    for (int g = 0; g < nchunks && !abort_flag; ++g) {
-      int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
-      for (int p = 0; p < plan.npass && !abort_flag; ++p)
-        for (int kb = kb0; kb < kb1; ++kb, ++it) {
-          int s = it % OZ_STAGES;
-          if (!mbar_wait(&empty[s], ((it / OZ_STAGES) & 1) ^ 1)) {
-            atomicExch(&abort_flag, 1);
-            break;
-          }
-          mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-          tma_load_4d(sA + s * A_BYTES, &mapA, &full[s], kb * BK, m0, a_batched ? b : 0, plan.pa[p]);
-          tma_load_4d(sB + s * B_BYTES, &mapB, &full[s], kb * BK, n0, b_batched ? b : 0, plan.pb[p]);
-          issued = it + 1;
-        }
+    int issued = 0;
+    for (int kb = 0; kb < kblocks && !abort_flag; ++kb) {
+      const int s = kb % OZ_STAGES;
+      if (!mbar_wait(&empty[s], ((kb / OZ_STAGES) & 1) ^ 1)) {
+        atomicExch(&abort_flag, 1);
+        break;
+      }
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      uint8_t *st = smem + s * STAGE_BYTES;
+#pragma unroll
+      for (int t = 0; t < S; ++t)
+        tma_load_4d(st + t * A_BYTES, &mapA, &full[s], kb * OZ_BK, m0, a_batched ? b : 0, t);
+#pragma unroll
+      for (int u = 0; u < S; ++u)
+        tma_load_4d(st + S * A_BYTES + u * B_BYTES, &mapB, &full[s], kb * OZ_BK, n0,
+                    b_batched ? b : 0, u);
+      issued = kb + 1;
     }
     if (abort_flag)
       for (int j = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); j < issued; ++j)
         mbar_wait(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1);
   } else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = instr_desc(OZ_BN);
-    int it = 0;
     bool ok = true;
     for (int g = 0; g < nchunks && ok; ++g) {
       if (g > 0 && !mbar_wait(acce, (g - 1) & 1)) {
@@ -386,36 +417,48 @@ __global__ void __launch_bounds__(192, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
-      int last_d = -1;
-      for (int p = 0; p < plan.npass && ok; ++p) {
-        const int d = plan.pd[p];
-        const bool fresh = d != last_d;  // first pass of this weight in the chunk
-        last_d = d;
-        for (int kb = kb0; kb < kb1; ++kb, ++it) {
-          int s = it % OZ_STAGES;
-          if (!mbar_wait(&full[s], (it / OZ_STAGES) & 1) || abort_flag) {
-            ok = false;
-            break;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          uint32_t a_addr = smem_u32(sA + s * A_BYTES), b_addr = smem_u32(sB + s * B_BYTES);
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk)
-            mma_bf16(tmem + (uint32_t)(d * OZ_BN), smem_desc(a_addr + kk * 32),
-                     smem_desc(b_addr + kk * 32), idesc, (fresh && kb == kb0 && kk == 0) ? 0u : 1u);
-          mma_commit(&empty[s]);
+      const int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
+      for (int kb = kb0; kb < kb1; ++kb) {
+        const int s = kb % OZ_STAGES;
+        if (!mbar_wait(&full[s], (kb / OZ_STAGES) & 1) || abort_flag) {
+          ok = false;
+          break;
         }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a_base = smem_u32(smem + s * STAGE_BYTES);
+        const uint32_t b_base = a_base + S * A_BYTES;
+#pragma unroll
+        for (int t = 0; t < S; ++t)
+#pragma unroll
+          for (int u = 0; u + t < S; ++u)
+#pragma unroll
+            for (int kk = 0; kk < OZ_BK / 16; ++kk)
+              // the first product into weight t+u in the chunk is (0, t+u) at kb0, kk 0
+              mma_bf16(tmem + (uint32_t)((t + u) * OZ_BN),
+                       smem_desc64(a_base + t * A_BYTES + kk * 32),
+                       smem_desc64(b_base + u * B_BYTES + kk * 32), idesc,
+                       (kb == kb0 && t == 0 && kk == 0) ? 0u : 1u);
+        mma_commit(&empty[s]);
       }
       mma_commit(accf);
     }
     if (!ok) atomicExch(&abort_flag, 1);
   } else if (warp >= 2) {
+    // Every chunk's FP32 sums are integers below 2^24, so the weights fold into one
+    // int64 per column by Horner in base 2^7: t = sum_d v_d 2^(7 (SI - 1 - d)) is exact
+    // for the first SI = min(S, 5) weights (|t| < 2^52 per chunk); a sixth weight is
+    // rounded to units of 2^7 first (2^-42 of the scaled product, below FP64 rounding
+    // of the result). The int64 sum over chunks is converted to FP64 once, at the end:
+    // the per-chunk work is integer, not FP64, arithmetic.
+    // Two warps per TMEM lane quarter (q = warp % 4), each owning half of the columns.
+    constexpr int SI = S < 5 ? S : 5;
+    constexpr int NC = OZ_BN / 2;
     const int q = warp & 3;
+    const int h = (warp - 2) / 4;
     const int m = m0 + q * 32 + lane;
-    double acc[OZ_BN];
+    long long acc[NC];
 #pragma unroll
-    for (int j = 0; j < OZ_BN; ++j) acc[j] = 0.0;
+    for (int j = 0; j < NC; ++j) acc[j] = 0;
     bool ok = true;
     for (int g = 0; g < nchunks && ok; ++g) {
       if (!mbar_wait(accf, g & 1) || abort_flag) {
@@ -424,14 +467,22 @@ __global__ void __launch_bounds__(192, 1)
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-      for (int d = 0; d < S; ++d) {
-        const double w = ldexp(1.0, -7 * (d + 2));
+      for (int c0 = 0; c0 < NC; c0 += 8) {
+        uint32_t r[S][8];
 #pragma unroll
-        for (int c0 = 0; c0 < OZ_BN; c0 += 16) {
-          float v[16];
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * OZ_BN + c0), v);
+        for (int d = 0; d < S; ++d)
+          tmem_ld8_issue(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * OZ_BN + h * NC + c0),
+                         r[d]);
+        tmem_ld_wait();
 #pragma unroll
-          for (int j = 0; j < 16; ++j) acc[c0 + j] += w * (double)v[j];
+        for (int j = 0; j < 8; ++j) {
+          long long t = 0;
+#pragma unroll
+          for (int d = 0; d < SI; ++d) t = t * 128 + (long long)__float2int_rn(__uint_as_float(r[d][j]));
+#pragma unroll
+          for (int d = SI; d < S; ++d)
+            t += (long long)__float2int_rn(__uint_as_float(r[d][j]) * exp2f(-7.0f * (d - SI + 1)));
+          acc[c0 + j] += t;
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -441,12 +492,12 @@ __global__ void __launch_bounds__(192, 1)
     if (!ok) atomicExch(&abort_flag, 1);
     double dot = 0.0;
     if (ok && m < M) {
-      const int er = epi.ea[(long long)b * epi.ea_sb + m];
+      const int er = epi.ea[(long long)b * epi.ea_sb + m] - 7 * (SI + 1);
 #pragma unroll
-      for (int j = 0; j < OZ_BN; ++j) {
-        int n = n0 + j;
+      for (int j = 0; j < NC; ++j) {
+        int n = n0 + h * NC + j;
         if (n < N) {
-          double cv = ldexp(acc[j], er + epi.eb[(long long)b * epi.eb_sb + n]);
+          double cv = ldexp((double)acc[j], er + epi.eb[(long long)b * epi.eb_sb + n]);
           long long o = (long long)b * epi.sb + m + (long long)n * epi.ldn;
           if (epi.mode == 0)
             epi.c[o] = cv;
@@ -464,7 +515,9 @@ __global__ void __launch_bounds__(192, 1)
   __syncthreads();
   if (epi.mode == 1 && threadIdx.x == 0) {
     long long cta = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
-    epi.partial[cta] = red[0] + red[1] + red[2] + red[3];
+    double sum = 0.0;
+    for (int w = 0; w < OZ_EPI_WARPS; ++w) sum += red[w];
+    epi.partial[cta] = sum;
   }
   if (threadIdx.x == 0 && abort_flag) atomicExch(err_flag, 1);
   if (warp == 1) {
@@ -721,9 +774,9 @@ OzPlan oz_plan(int precision) {
     }
   p.npass = n;
   // exact FP32 partial sums: (S+2) 2^12 c < 2^24 and 2^14 c < 2^24
-  int c = (4096 / (p.S + 2)) / BK * BK;
-  if ((long long)(p.S + 2) * 4096 * c >= (1ll << 24)) c -= BK;
-  p.chunk_kb = c / BK;
+  int c = (4096 / (p.S + 2)) / OZ_BK * OZ_BK;
+  if ((long long)(p.S + 2) * 4096 * c >= (1ll << 24)) c -= OZ_BK;
+  p.chunk_kb = c / OZ_BK;
   return p;
 }
 
@@ -757,17 +810,18 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
   cuuint64_t dims[4] = {(cuuint64_t)op.Kp, (cuuint64_t)rows, (cuuint64_t)nb, (cuuint64_t)S};
   cuuint64_t strides[3] = {(cuuint64_t)op.Kp * 2, (cuuint64_t)rows * op.Kp * 2,
                            (cuuint64_t)nb * rows * op.Kp * 2};
-  cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1, 1};
+  cuuint32_t box[4] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1, 1};
   cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = enc(&op.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, op.buf.p, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   return GC_OK;
 }
 
-size_t oz_smem_bytes() {
-  return 1024 + OZ_STAGES * (size_t)(BM * BK * 2 + OZ_BN * BK * 2) + (2 * OZ_STAGES + 2) * 8 + 16;
+size_t oz_smem_bytes(int S) {
+  return 1024 + OZ_STAGES * (size_t)S * (BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) +
+         (2 * OZ_STAGES + 2) * 8 + 16;
 }
 
 template <int S>
@@ -777,12 +831,12 @@ int launch_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, in
   static cudaError_t cfg = cudaSuccess;
   std::call_once(once, [] {
     cfg = cudaFuncSetAttribute(k_tc_gemm_oz<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)oz_smem_bytes());
+                               (int)oz_smem_bytes(S));
   });
   GC_CUDA(ctx, cfg);
   dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, OZ_BN), nbatch);
-  k_tc_gemm_oz<S><<<grid, 192, oz_smem_bytes(), ctx->stream>>>(
-      A.map, B.map, M, N, A.Kp / BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag);
+  k_tc_gemm_oz<S><<<grid, OZ_THREADS, oz_smem_bytes(S), ctx->stream>>>(
+      A.map, B.map, M, N, A.Kp / OZ_BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag);
   GC_LAUNCHED(ctx);
   return GC_OK;
 }
