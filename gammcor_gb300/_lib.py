@@ -42,6 +42,7 @@ SIGNATURES = {
     "gc_kernel_launches": (C.c_longlong, [_vp]),
     "gc_set_eig_emulation": (C.c_int, [_vp, C.c_int]),
     "gc_set_eig_refinement": (C.c_int, [_vp, C.c_int]),
+    "gc_set_chol_blocked": (C.c_int, [_vp, C.c_int]),
     "gc_eig_refine_stats": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]),
     "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),

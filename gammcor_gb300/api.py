@@ -61,6 +61,10 @@ class Context:
         """Refinement iterations of the refined ERPA form (1..4)."""
         check(self.h, load().gc_set_eig_refinement(self.h, int(iterations)))
 
+    def set_chol_blocked(self, on: bool):
+        """Blocked Cholesky of A+B with tensor-core trailing updates (N >= 1536)."""
+        check(self.h, load().gc_set_chol_blocked(self.h, int(on)))
+
     def eig_refine_stats(self) -> dict:
         """Refined ERPA counters: solves, dsyevd fallbacks, largest block cluster."""
         s, f, m = C.c_longlong(), C.c_longlong(), C.c_int()

@@ -130,6 +130,8 @@ int syevd(gc_context *ctx, int N, double *A, double *w) {
 // so rotations inside a cluster of (near-)equal eigenvalues do not matter; the
 // block solve only has to be exact.
 constexpr int kMaxCluster = 64;
+constexpr int kCholBlock = 256;        // blocked Cholesky: diagonal block order
+constexpr int kCholBlockedMin = 1536;  // below this order one dpotrf call is faster
 constexpr double kTau = 0.05;
 
 __global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
@@ -633,6 +635,82 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
   return GC_OK;
 }
 
+// One dpotrf over the lower triangle of A; *minor as in chol_blocked.
+int chol_plain(gc_context *ctx, int N, double *A, int *minor) {
+  *minor = 0;
+  int lwork = 0;
+  GC_CUSOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, N, A, N,
+                                               &lwork));
+  gc::DevBuf<double> work;
+  GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
+  GC_CUSOLVER(ctx, cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, N, A, N, work.p, lwork,
+                                    ctx->dev_info));
+  int info = 0;
+  GC_CUDA(ctx, cudaMemcpyAsync(&info, ctx->dev_info, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (info < 0) return gc::set_error(ctx, GC_ECUSOLVER, "potrf info=%d", info);
+  *minor = info;
+  return GC_OK;
+}
+
+// A22 -= T on the lower triangle (A22 column-major with leading dimension lda,
+// T m x m with leading dimension m).
+__global__ void k_sub_lower(int m, double *__restrict__ A22, long long lda,
+                            const double *__restrict__ T) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (i >= m || i < j) return;
+  A22[i + (size_t)j * lda] -= T[i + (size_t)j * m];
+}
+
+// Blocked right-looking Cholesky of the lower triangle of A (N x N, column-major):
+// diagonal blocks by dpotrf (FP64), panels by dtrsm (FP64), trailing updates
+// A22 -= P P^T with the sliced tensor-core GEMM of precision prec (L L^T then
+// equals A to that product's ~2^-35 relative error). *minor = 0 on success, else
+// the order of the leading minor that is not positive definite.
+int chol_blocked(gc_context *ctx, int N, double *A, int prec, int nb, int *minor) {
+  *minor = 0;
+  const int nblk = (N + nb - 1) / nb;
+  gc::DevBuf<int> infos;
+  gc::DevBuf<double> T, work;
+  GC_TRY(infos.alloc(ctx, nblk));
+  GC_CUDA(ctx, cudaMemsetAsync(infos.p, 0, nblk * sizeof(int), ctx->stream));
+  const int m1 = N - nb;
+  if (m1 > 0) GC_TRY(T.alloc(ctx, (size_t)m1 * m1));
+  int lwork = 0;
+  GC_CUSOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, nb, A, N,
+                                               &lwork));
+  GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
+  const double one = 1.0;
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int k0 = blk * nb, kb = std::min(nb, N - k0), m = N - k0 - kb;
+    double *A11 = A + k0 + (size_t)k0 * N;
+    GC_CUSOLVER(ctx, cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, kb, A11, N, work.p,
+                                      lwork, infos.p + blk));
+    if (m == 0) break;
+    double *P = A11 + kb;  // rows k0+kb.., columns k0..k0+kb
+    GC_CUBLAS(ctx, cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                               CUBLAS_DIAG_NON_UNIT, m, kb, &one, A11, N, P, N));
+    GC_TRY(gc::tc_gemm_strided(ctx, prec, m, m, kb, P, 1, N, P, 1, N, T.p, m));  // T = P P^T
+    k_sub_lower<<<dim3(gc::ceil_div(m, 256), m), 256, 0, ctx->stream>>>(
+        m, A + (k0 + kb) + (size_t)(k0 + kb) * N, N, T.p);
+    GC_LAUNCHED(ctx);
+  }
+  std::vector<int> h(nblk);
+  GC_CUDA(ctx, cudaMemcpyAsync(h.data(), infos.p, nblk * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int blk = 0; blk < nblk; ++blk) {
+    if (h[blk] < 0) return gc::set_error(ctx, GC_ECUSOLVER, "potrf info=%d", h[blk]);
+    if (h[blk] > 0) {  // later blocks worked on an invalid update: report the first
+      *minor = blk * nb + h[blk];
+      break;
+    }
+  }
+  return GC_OK;
+}
+
 // Eigenpairs of the symmetric M in place (vectors overwrite M, values in w):
 // dsyevd, or the refined FP32 solve with dsyevd as its fallback.
 int eigen(gc_context *ctx, int N, double *M, double *w, int mode, int prec) {
@@ -698,22 +776,14 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_TRY(M.alloc(ctx, NN));
     GC_CUDA(ctx, cudaMemcpyAsync(L.p, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
-    int lwork = 0;
-    GC_CUSOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, N, L.p, N,
-                                                 &lwork));
-    {
-      DevBuf<double> work;
-      GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
-      GC_CUSOLVER(ctx, cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, N, L.p, N, work.p,
-                                        lwork, ctx->dev_info));
-      int info = 0;
-      GC_CUDA(ctx, cudaMemcpyAsync(&info, ctx->dev_info, sizeof(int), cudaMemcpyDeviceToHost,
-                                   ctx->stream));
-      GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      if (info > 0)
-        return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", info);
-      if (info < 0) return set_error(ctx, GC_ECUSOLVER, "potrf info=%d", info);
-    }
+    const bool tc_prec = gemm_precision == GC_PREC_FP64TC5 || gemm_precision == GC_PREC_FP64TC6;
+    int minor = 0;
+    if (tc_prec && ctx->chol_blocked && N >= kCholBlockedMin)
+      GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, kCholBlock, &minor));
+    else
+      GC_TRY(chol_plain(ctx, N, L.p, &minor));
+    if (minor > 0)
+      return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
     k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
     GC_LAUNCHED(ctx);
     const bool tc = gemm_precision == GC_PREC_FP64TC5 || gemm_precision == GC_PREC_FP64TC6;
@@ -771,6 +841,12 @@ extern "C" int gc_set_eig_refinement(gc_context *ctx, int iterations) {
   if (iterations < 1 || iterations > 4)
     return gc::set_error(ctx, GC_EINVAL, "refinement iterations %d outside 1..4", iterations);
   ctx->eig_refine = iterations;
+  return GC_OK;
+}
+
+extern "C" int gc_set_chol_blocked(gc_context *ctx, int on) {
+  if (!ctx) return GC_EINVAL;
+  ctx->chol_blocked = on ? 1 : 0;
   return GC_OK;
 }
 

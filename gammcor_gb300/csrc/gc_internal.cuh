@@ -26,6 +26,7 @@ struct gc_context {
   long long refine_solves = 0;       // GC_ERPA_CHOLESKY_REFINED solves
   long long refine_fallbacks = 0;    // of which fell back to dsyevd
   int refine_max_cluster = 0;        // largest cluster diagonalised in a block
+  int chol_blocked = 1;              // blocked Cholesky with tensor-core trailing updates
   std::string err;
 };
 

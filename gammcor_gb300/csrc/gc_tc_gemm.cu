@@ -544,6 +544,21 @@ __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, in
   }
 }
 
+// Balanced base-128 digits of n = rint(x 2^(7S - e)) (|n| < 2^(7S) since |x| < 2^e):
+// n = sum_s a_s 128^(S-1-s), |a_0| <= 128, |a_s| <= 64 otherwise; plane s gets a_s.
+// One FP64 scaling and one conversion per element, the digits in integer arithmetic
+// (the FP64 pipe is the narrow one on this part).
+__device__ __forceinline__ void store_digits(double x, int e, int S, long long plane, long long o,
+                                             __nv_bfloat16 *__restrict__ planes) {
+  long long n = __double2ll_rn(ldexp(x, 7 * S - e));
+  for (int s = S - 1; s > 0; --s) {
+    const long long d = ((n + 64) & 127) - 64;
+    planes[s * plane + o] = __float2bfloat16_rn((float)d);
+    n = (n - d) >> 7;
+  }
+  planes[o] = __float2bfloat16_rn((float)n);
+}
+
 // Integer slices: planes[t][b][r][kp] = alpha_t of x[b,r,k] 2^-e[b][r].
 __global__ void k_slice_planes(const double *__restrict__ x, int rows, int K, int Kp, int nb,
                                long long sr, long long sk, long long sb, int S,
@@ -555,13 +570,8 @@ __global__ void k_slice_planes(const double *__restrict__ x, int rows, int K, in
     long long rr = t / Kp;
     int r = (int)(rr % rows);
     long long bb = rr / rows;
-    double v = k < K ? ldexp(x[bb * sb + (long long)r * sr + (long long)k * sk], -e[rr]) : 0.0;
-    for (int s = 0; s < S; ++s) {
-      v *= 128.0;
-      double a = rint(v);
-      v -= a;
-      planes[s * plane + t] = __double2bfloat16(a);
-    }
+    const double xv = k < K ? x[bb * sb + (long long)r * sr + (long long)k * sk] : 0.0;
+    store_digits(xv, e[rr], S, plane, t, planes);
   }
 }
 
@@ -581,14 +591,8 @@ __global__ void k_slice_planes_t(const double *__restrict__ x, int rows, int K, 
   for (int i = ty; i < 32; i += 8) {
     int r = r0 + i, k = k0 + tx;
     if (r >= rows || k >= Kp) continue;
-    double v = ldexp(tile[tx][i], -e[(long long)bb * rows + r]);
-    long long o = ((long long)bb * rows + r) * Kp + k;
-    for (int s = 0; s < S; ++s) {
-      v *= 128.0;
-      double a = rint(v);
-      v -= a;
-      planes[s * plane + o] = __double2bfloat16(a);
-    }
+    const long long o = ((long long)bb * rows + r) * Kp + k;
+    store_digits(tile[tx][i], e[(long long)bb * rows + r], S, plane, o, planes);
   }
 }
 

@@ -73,6 +73,10 @@ long long gc_kernel_launches(const gc_context *ctx);
 int gc_set_eig_emulation(gc_context *ctx, int on);
 /* Refinement iterations of GC_ERPA_CHOLESKY_REFINED (default 2, range 1..4). */
 int gc_set_eig_refinement(gc_context *ctx, int iterations);
+/* on = 1 (default): the Cholesky of A+B in the ERPA forms with sliced tensor-core
+ * products is blocked (order 256 diagonal blocks by dpotrf, panels by dtrsm,
+ * trailing updates on the sliced GEMM) for N >= 1536; on = 0: one FP64 dpotrf. */
+int gc_set_chol_blocked(gc_context *ctx, int on);
 /* Counters of GC_ERPA_CHOLESKY_REFINED on a context: solves, solves that fell back to
  * dsyevd, and the largest cluster of close eigenvalues diagonalised in a block. */
 int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,

@@ -173,3 +173,45 @@ def test_refined_batch_agrees_with_fp64_on_larger_systems(gpu_lib):
     assert err < 1e-8, err
     st = ctx.eig_refine_stats()
     assert st["solves"] == 16 and st["fallbacks"] == 0, st
+
+
+def spd(N, seed, lo=1.0, hi=1e3, negative=0):
+    """Q diag(ev) Q^T with ev geometric in [lo, hi]; the first `negative` set to -1."""
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.normal(size=(N, N)))
+    ev = np.geomspace(lo, hi, N)
+    ev[:negative] = -1.0
+    A = (Q * ev) @ Q.T
+    return 0.5 * (A + A.T)
+
+
+def test_blocked_cholesky_matches_plain_and_numpy(gpu_lib):
+    """N = 1800 is above the blocked-Cholesky threshold: A+ = L L^T with tensor-core
+    trailing updates gives the omega and sum y y^T of the single-dpotrf form and of
+    numpy. Both forms build L^T A- L from FP64TC5 products (~2^-35 of |A||B| per
+    element); with |L^T A- L| <= 50 and omega^2 >= 0.5 that moves omega by ~1e-8
+    relative, checked at 1e-6."""
+    N = 1800
+    ap, am = spd(N, 1, 1.0, 10.0), spd(N, 2, 0.5, 5.0)
+    res = []
+    for blocked in (True, False):
+        ctx = api.Context(0)
+        ctx.set_chol_blocked(blocked)
+        y, e = api.erpasymm1(t(ap), t(am), mode="refined", precision="fp64tc5", ctx=ctx)
+        res.append((np.sort(e.cpu().numpy()), yyT(y.cpu().numpy(), e.cpu().numpy())))
+    L = np.linalg.cholesky(ap)
+    om = np.sqrt(np.linalg.eigvalsh(L.T @ am @ L))
+    for e, _ in res:
+        np.testing.assert_allclose(e, om, rtol=1e-6)
+    assert np.abs(res[0][1] - res[1][1]).max() < 1e-6 * np.abs(res[1][1]).max()
+
+
+@pytest.mark.parametrize("blocked", [True, False])
+def test_cholesky_reports_not_positive_definite(gpu_lib, blocked):
+    N = 1700
+    ap, am = spd(N, 3, negative=1), spd(N, 4)
+    ctx = api.Context(0)
+    ctx.set_chol_blocked(blocked)
+    with pytest.raises(GcError) as ei:
+        api.erpasymm1(t(ap), t(am), mode="refined", precision="fp64tc5", ctx=ctx)
+    assert ei.value.code == 5  # GC_ENOTPD
