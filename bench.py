@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--kernel-only", type=int, default=0,
                     help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--erpa-once", action="store_true",
+                    help="time one ERPA solve (the --erpa form) of the largest batch system, "
+                         "inside a profiler range (for profiling)")
     return ap.parse_args()
 
 
@@ -222,6 +225,36 @@ def run_ours(args):
     __graft_entry__.build()
     from gammcor_gb300 import api, surrogate
 
+    if args.erpa_once:
+        from gammcor_gb300 import synth
+        shapes = synth.batched_shapes(args.nsys, args.seed)
+
+        def pairs(sh):
+            nv = sh["n"] - sh["nin"] - sh["nact"]
+            return sh["n"] * (sh["n"] - 1) // 2 - sh["nin"] * (sh["nin"] - 1) // 2 - nv * (nv - 1) // 2
+        sh = max(shapes, key=pairs)
+        s = synth.make_system_device(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"],
+                                     device=dev)
+        C = torch.as_tensor(np.asfortranarray(s.cmo), device=dev)
+        L = torch.as_tensor(np.asfortranarray(s.lfac), device=dev)
+        co = C[:, :s.nocc].contiguous()
+        indn = api.pair_space(s.occ, s.nele)
+        fofo = api.tran4_factored(s.n, L, C, co, C, co, precision=args.precision)
+        ffoo = api.tran4_factored(s.n, L, co, co, C, C, precision=args.precision)
+        abp, abm, _ = api.ab_cas_fofo(s.occ, s.xone, indn, s.nact, s.nin, ffoo, fofo, s.rdm2act, 0.5)
+        api.erpasymm1(abp.clone(), abm.clone(), mode=args.erpa, precision=args.precision)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.cudart().cudaProfilerStart()
+        e0.record()
+        api.erpasymm1(abp, abm, mode=args.erpa, precision=args.precision)
+        e1.record()
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStop()
+        print(json.dumps({"erpa": args.erpa, "precision": args.precision, "N": len(indn),
+                          "ms": e0.elapsed_time(e1)}))
+        return
+
     if args.kernel_only:
         n = args.kernel_only
         ms_k = api.tc_gemm_time(n, n, n, args.precision, reps=3)
@@ -320,8 +353,14 @@ def run_ours(args):
     npass = {"bf16x3": 3, "bf16x6": 6, "fp64tc5": 15, "fp64tc6": 21}[args.precision]
     ms_k = api.tc_gemm_time(Nmax, Nmax, Nmax, args.precision, reps=5)
     ach = 2.0 * Nmax ** 3 * npass / (ms_k / 1000.0) / 1e12
+    # DRAM bytes (read + write) of one 4096^3 FP64TC5 launch from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum = 2.5430 GB + 0.1375 GB), scaled
+    # to this launch by the units processed (operand tiles re-read per output tile:
+    # proportional to M N K at equal L2 hit rate).
+    traffic = 2.6806e9 * (Nmax / 4096.0) ** 3 if args.precision == "fp64tc5" else None
     roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-            "frac": ach / bf16, "traffic": None, "peak_source": src,
+            "frac": ach / bf16, "traffic": traffic, "traffic_unit": "bytes",
+            "traffic_source": "ncu, 4096^3 launch scaled by (N/4096)^3", "peak_source": src,
             "kernel": f"tcgen05 GEMM ({args.precision}) {Nmax}^3 x {npass} BF16 passes, "
                       f"{ms_k:.2f} ms/launch"}
 
