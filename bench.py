@@ -79,6 +79,30 @@ def dist_env():
     return world, rank, local
 
 
+def rank_shapes(nsys: int, seed: int, rank: int):
+    """One rank's batch: the shared shape distribution with the rank's own seeds.
+    Systems are independent and no system is on two ranks, so the ranks exchange
+    no data (weak scaling); only the timing reduction is collective."""
+    from gammcor_gb300 import synth
+    return synth.batched_shapes(count=nsys, seed=seed + 7919 * rank)
+
+
+def max_over_ranks(values, world: int, device):
+    """Element-wise maximum of per-rank timings over all ranks."""
+    if world == 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def whole_job_rate(world: int, nsys: int, ms: float) -> float:
+    """Energies per second of the whole job: every rank's systems over the slowest rank."""
+    return world * nsys / (ms / 1000.0)
+
+
 def read_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -142,7 +166,7 @@ def make_batch(nsys, seed, device, run, rank_offset=0, log=print, gen="device"):
     quadrature point are reported by the GPU path itself (Cholesky status) and
     resampled; the final check run is the first warm-up step on the final batch."""
     from gammcor_gb300 import api, synth
-    shapes = synth.batched_shapes(count=nsys, seed=seed + 7919 * rank_offset)
+    shapes = rank_shapes(nsys, seed, rank_offset)
     if gen == "device":
         make = lambda n, a, b, r, sd: synth.make_system_device(n, a, b, r, sd, device=device)  # noqa
     else:
@@ -315,12 +339,9 @@ def run_ours(args):
     ms /= args.steps
     ems /= args.steps
     launches = (ctx.launches() - l0) // args.steps
-    if world > 1:
-        t = torch.tensor([ms, ems], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, ems = float(t[0]), float(t[1])
-    value = world * args.nsys / (ms / 1000.0)
-    e2e = {"value": world * args.nsys / (ems / 1000.0), "unit": "energies/s",
+    ms, ems = max_over_ranks([ms, ems], world, dev)
+    value = whole_job_rate(world, args.nsys, ms)
+    e2e = {"value": whole_job_rate(world, args.nsys, ems), "unit": "energies/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     log(f"step: {ms:.0f} ms, {value:.3f} energies/s (e2e {e2e['value']:.3f}), fallback "
         f"{fb.mean():.2f}, {launches} kernels/step")
