@@ -407,8 +407,10 @@ def run_ours(args):
                            "eig_emulation": bool(args.eig_emulation),
                            "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"},
                 "surrogate_fallback_rate": float(fb.mean()),
-                "plain_fp64_subset": {"systems": sub, "plain_s": t_plain, "step_s": t_fast_sub,
-                                      "speedup": t_plain / t_fast_sub,
+                "plain_fp64_subset": {"systems": sub,
+                                      "plain_s": t_plain if sub else None,
+                                      "step_s": t_fast_sub if sub else None,
+                                      "speedup": t_plain / t_fast_sub if sub else None,
                                       "max_abs_err_eh": float(err.max()),
                                       "within_1ueh": bool(err.max() <= 1e-6)},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
