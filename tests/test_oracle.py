@@ -145,3 +145,32 @@ def test_golden_fixture_reproduces():
     x, w = R.gauleg(0.0, 1.0, int(d["ngrid"]))
     np.testing.assert_allclose(x, d["x"], atol=1e-15)
     assert abs(np.dot(w, d["w_lambda"]) - float(d["ecorr"])) < 1e-12
+
+
+@pytest.mark.parametrize("cfg", [dict(n=14, nin=0, nact=4, rank=50),   # no inactive orbitals
+                                 dict(n=14, nin=3, nact=2, rank=50),   # CAS(2,2)
+                                 dict(n=12, nin=2, nact=6, rank=40)])  # CAS(6,6)
+def test_edge_shapes_fofo_equals_incore(cfg):
+    """Shapes at the edges of the configs: E_CAS equals the CI energy, the FOFO
+    assembly and integrand equal the in-core restatement, and a one-point rule is
+    W(1/2)."""
+    s = synth.make_system(**cfg, seed=1)
+    G, ffoo, fofo = oracle_integrals(s)
+    n = s.n
+    indn = R.pair_space(s.occ, s.nele)
+    V = synth.mo_eri_from_factor(s.lfac, n, s.cmo, s.cmo, s.cmo, s.cmo)
+    abp, abm, e1 = R.ab_cas_fofo(s.occ, s.xone, np.eye(n), indn, s.nin, s.nact, ffoo, fofo,
+                                 s.rdm2act, 0.5)
+    bp, bm, e2 = IC.ab_cas_incore(V, s.occ, synth.unpack_sym(s.xone, n),
+                                  synth.unpack_rdm2act(s.rdm2act, s.nact), s.nin, s.nact, indn, 0.5)
+    scale = max(np.abs(abp).max(), np.abs(abm).max())
+    assert np.abs(abp - bp).max() < 1e-12 * scale and np.abs(abm - bm).max() < 1e-12 * scale
+    assert abs(e1 - s.e_cas) < 1e-10 and abs(e2 - s.e_cas) < 1e-10
+    Y, eig, _ = R.erpasymm1(abp, abm)
+    w1 = R.ac_ene_erpa_fofo(Y, eig, s.occ, s.nin, s.nact, indn, fofo)
+    w2 = IC.ac_ene_erpa_incore(V, Y, eig, s.occ, s.nin, s.nact, indn)
+    assert abs(w1 - w2) < 1e-12 * max(1.0, abs(w1))
+    ecas, ecorr, ws, x, w = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act,
+                                      ngrid=1)
+    assert x[0] == pytest.approx(0.5) and w[0] == pytest.approx(1.0)
+    assert abs(ecorr - w1) < 1e-12 * max(1.0, abs(w1))
