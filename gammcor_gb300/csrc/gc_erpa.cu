@@ -25,6 +25,14 @@ __global__ void k_symmetrize(int N, double *__restrict__ a) {
   a[l] = v;
 }
 
+// Copy the lower triangle onto the upper one.
+__global__ void k_mirror_lower(int N, double *__restrict__ a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= N || j <= i) return;
+  a[i + (size_t)j * N] = a[j + (size_t)i * N];
+}
+
 // Copy the upper triangle onto the lower one.
 __global__ void k_mirror_upper(int N, double *__restrict__ a) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -578,11 +586,21 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
   for (int it = 0; it < iters; ++it) {
     double *X = cur, *P = cur + NN, *G = nxt, *S = nxt + NN;
     GC_TRY(product(ctx, prec, false, N, N, N, M, N, X, N, P, N));        // P = M X
-    GC_TRY(product(ctx, prec, true, N, 2 * N, N, X, N, X, N, G, N));     // [G S] = X^T [X P]
-    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, G);
-    GC_LAUNCHED(ctx);
-    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, S);
-    GC_LAUNCHED(ctx);
+    // [G S] = X^T [X P]; both blocks are symmetric, so on the tensor-core path only
+    // their lower triangles are computed and mirrored
+    if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6) {
+      GC_TRY(gc::tc_gemm_strided_lower(ctx, prec, N, 2 * N, N, X, N, 1, X, N, 1, G, N, N));
+      k_mirror_lower<<<g2, b2, 0, ctx->stream>>>(N, G);
+      GC_LAUNCHED(ctx);
+      k_mirror_lower<<<g2, b2, 0, ctx->stream>>>(N, S);
+      GC_LAUNCHED(ctx);
+    } else {
+      GC_TRY(product(ctx, prec, true, N, 2 * N, N, X, N, X, N, G, N));
+      k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, G);
+      GC_LAUNCHED(ctx);
+      k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, S);
+      GC_LAUNCHED(ctx);
+    }
     k_rayleigh<<<gN, 256, 0, ctx->stream>>>(N, G, S, lam, nullptr, nullptr);
     GC_LAUNCHED(ctx);
     k_col_coupling<<<N, 256, 0, ctx->stream>>>(N, G, S, lam, colm.p);

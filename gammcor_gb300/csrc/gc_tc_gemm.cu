@@ -339,6 +339,8 @@ struct OzEpi {
   const int *ea;         // row exponents of A, [batch][rows] (batch stride 0 if shared)
   const int *eb;         // row exponents of B
   long long ea_sb, eb_sb;
+  int tri_period;        // > 0: skip tiles wholly above the diagonal of each
+                         // tri_period-wide column block (C lower-triangular per block)
 };
 
 template <int S>
@@ -364,6 +366,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * OZ_BN, b = blockIdx.z;
   const int nchunks = (kblocks + plan.chunk_kb - 1) / plan.chunk_kb;
+  if (epi.tri_period > 0) {  // whole CTA, before any barrier or TMEM is set up
+    const int c0 = n0 % epi.tri_period;
+    if (c0 + OZ_BN <= epi.tri_period && c0 >= m0 + BM) return;
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < OZ_STAGES; ++s) {
@@ -943,6 +949,20 @@ int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const d
   GC_TRY(make_oz_operand(ctx, a, A, M, K, 1, sam, sak, 0, pl.S, BM));
   GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+  GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
+  return check_flag(ctx);
+}
+
+int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, const double *A,
+                          long long sam, long long sak, const double *B, long long sbn,
+                          long long sbk, double *C, long long ldc, int period) {
+  if (!is_oz(precision))
+    return set_error(ctx, GC_EINVAL, "gemm_strided_lower: needs a sliced FP64-accurate precision");
+  OzPlan pl = oz_plan(precision);
+  OzOperand a, b;
+  GC_TRY(make_oz_operand(ctx, a, A, M, K, 1, sam, sak, 0, pl.S, BM));
+  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
+  OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, period};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
   return check_flag(ctx);
 }

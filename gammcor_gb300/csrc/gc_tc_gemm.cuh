@@ -27,6 +27,13 @@ int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const d
                     long long sam, long long sak, const double *B, long long sbn, long long sbk,
                     double *C, long long ldc);
 
+// As tc_gemm_strided, computing only the tiles of C that reach the lower triangle
+// (diagonal included) of each `period`-wide column block; the rest of C is not
+// written (for products known to be symmetric in each block).
+int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, const double *A,
+                          long long sam, long long sak, const double *B, long long sbn,
+                          long long sbk, double *C, long long ldc, int period);
+
 int fp64_two_sided(gc_context *ctx, int n, int cnt, const double *M, int nX, const double *CX,
                    int nY, const double *CY, double *T1, double *out, long long ostride);
 
