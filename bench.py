@@ -66,6 +66,13 @@ def parse():
     ap.add_argument("--kernel-only", type=int, default=0,
                     help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="batched", choices=["batched", "precision", "large"],
+                    help="batched: the 64-system batch (the headline); precision: the "
+                         "transform-scale precision study (n=400, 40 inactive, CAS(8,8), rank "
+                         "2400); large: the large single system (n=500, 30 inactive, CAS(8,8), "
+                         "rank 3000)")
+    ap.add_argument("--plain", type=int, default=0,
+                    help="large workload: also time the plain FP64 GPU path (ERPASYMM1)")
     ap.add_argument("--erpa-once", action="store_true",
                     help="time one ERPA solve (the --erpa form) of the largest batch system, "
                          "inside a profiler range (for profiling)")
@@ -421,9 +428,109 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_single(args):
+    """The single-system configurations.
+
+    precision: the FFOO/FOFO transform in BF16x3, BF16x6 and FP64TC5 against the
+    FP64 transform (max abs integral error), and the AC energy of each set of
+    integrals with the assembly in FP64 and the ERPA eigenpairs and integrand
+    FP64-accurate (refined form, FP64TC6 products), so that the energy error is
+    the transform's.
+
+    large: the measured form on one system (FP64TC5 products, refined ERPA, the
+    surrogate gate with its fallback), its time per energy, and its error against
+    the same quadrature with FP64TC6 products; --plain 1 adds the plain FP64 GPU
+    path (ERPASYMM1 with FP64 products, minutes at this size)."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    dev = "cuda:0"
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
+    import __graft_entry__
+    __graft_entry__.build()
+    from gammcor_gb300 import api, surrogate, synth
+    cfg = dict(synth.CFG_PRECISION if args.workload == "precision" else synth.CFG_LARGE)
+    t0 = time.time()
+    s = synth.make_system_device(**cfg, seed=args.seed, device=dev)
+    batch = api.BatchInputs([s], dev)
+    N = int(batch.ndimx()[0])
+    log(f"system {cfg} N={N} generated in {time.time() - t0:.0f}s")
+    x8, w8 = surrogate.gauss8()
+    line = {"workload": args.workload, "system": cfg, "ndimx": N, "lambda_points": 8,
+            "data": "synthetic", "seed": args.seed}
+
+    def seconds(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1000.0, out
+
+    if args.workload == "precision":
+        C = torch.as_tensor(np.ascontiguousarray(s.cmo), device=dev)
+        L = torch.as_tensor(np.ascontiguousarray(s.lfac), device=dev)
+        co = C[:, :s.nocc].contiguous()
+        indn = batch.indn[0]
+
+        def transform(p):
+            fofo = api.tran4_factored(s.n, L, C, co, C, co, precision=p)
+            ffoo = api.tran4_factored(s.n, L, co, co, C, C, precision=p)
+            return fofo, ffoo
+
+        def energy(fofo, ffoo):
+            ws = []
+            for lam in x8:
+                abp, abm, ecas = api.ab_cas_fofo(s.occ, s.xone, indn, s.nact, s.nin, ffoo, fofo,
+                                                 s.rdm2act, float(lam))
+                y, e = api.erpasymm1(abp, abm, mode="refined", precision="fp64tc6")
+                ws.append(api.ace_ne_erpa_fofo(y, e, s.occ, indn, s.nact, s.nin, fofo,
+                                               precision="fp64tc6"))
+            return float(np.dot(w8, ws)), ecas
+
+        t64, (fofo64, ffoo64) = seconds(lambda: transform("fp64"))
+        e64, ecas = energy(fofo64, ffoo64)
+        res = {"fp64": {"transform_s": t64, "ecorr": e64, "integral_max_abs_err": 0.0,
+                        "ecorr_err": 0.0}}
+        for p in ("bf16x3", "bf16x6", "fp64tc5"):
+            tp, (fofo, ffoo) = seconds(lambda: transform(p))
+            err = max(float((fofo - fofo64).abs().max()), float((ffoo - ffoo64).abs().max()))
+            ep, _ = energy(fofo, ffoo)
+            res[p] = {"transform_s": tp, "ecorr": ep, "integral_max_abs_err": err,
+                      "ecorr_err": abs(ep - e64)}
+            log(f"{p}: transform {tp:.2f}s, max |d integral| {err:.2e}, |d Ecorr| {abs(ep - e64):.2e}")
+            del fofo, ffoo
+        line.update({"metric": "AC-CAS transform precision: max abs integral error and energy "
+                               "error vs FP64", "ecas": ecas, "results": res})
+    else:
+        ens = surrogate.Ensemble.load(surrogate.MODEL)
+        kw = dict(nstreams=1, precision="fp64tc5", erpa_mode="refined")
+        surrogate.energies(batch, ens, threshold=args.threshold, **kw)  # warm-up
+        t_fast, (e, fb, est, st) = seconds(lambda: surrogate.energies(batch, ens,
+                                                                       threshold=args.threshold,
+                                                                       **kw))
+        t_ref, ref = seconds(lambda: api.ac_energy_batched(batch, ngrid=8, precision="fp64tc6",
+                                                           erpa_mode="refined", nstreams=1))
+        line.update({"metric": "AC-CAS seconds per energy, large single system",
+                     "seconds_per_energy": t_fast, "ecorr": float(e[0]),
+                     "surrogate_fallback": bool(fb[0]), "status": int(st[0]),
+                     "reference_fp64tc6_s": t_ref, "ecorr_err_vs_fp64tc6": abs(float(e[0] - ref[0][0]))})
+        if args.plain:
+            t_plain, pl = seconds(lambda: api.ac_energy_batched(
+                batch, ngrid=8, precision="fp64", erpa_mode="symm1", affine=False, nstreams=1))
+            line.update({"plain_fp64_s": t_plain, "speedup_vs_plain": t_plain / t_fast,
+                         "ecorr_err_vs_plain": abs(float(e[0] - pl[0][0]))})
+        log(f"large: {t_fast:.1f}s per energy, fallback {bool(fb[0])}, "
+            f"|dE| vs FP64TC6 {line['ecorr_err_vs_fp64tc6']:.2e}")
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload != "batched":
+        run_single(a)
     else:
         run_ours(a)
