@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nsys", type=int, default=64)
     ap.add_argument("--ngrid", type=int, default=8)
-    ap.add_argument("--nstreams", type=int, default=8)
+    ap.add_argument("--nstreams", type=int, default=8,
+                    help="worker streams of the batch; 0 chooses them with api.autotune_streams")
     ap.add_argument("--precision", default="fp64tc5")
     ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
@@ -293,7 +294,7 @@ def run_ours(args):
         return
 
     ens = surrogate.Ensemble.load(surrogate.MODEL) if args.surrogate else None
-    kw = dict(nstreams=args.nstreams, precision=args.precision,
+    kw = dict(nstreams=args.nstreams or 8, precision=args.precision,
               eig_emulation=bool(args.eig_emulation), erpa_mode=args.erpa)
 
     def step(b):
@@ -310,6 +311,13 @@ def run_ours(args):
     log(f"batch ready in {time.time() - t0:.1f}s (includes the first warm-up step)")
     ctx = api.default_context(local)
     Ns = batch.ndimx()
+    tuned = None
+    if args.nstreams == 0:
+        best, times = api.autotune_streams(batch, precision=args.precision, erpa_mode=args.erpa)
+        tuned = {"streams": best, "seconds": {str(k): v for k, v in times.items()}}
+        kw["nstreams"] = best
+        args.nstreams = best
+        log(f"autotuned worker streams: {best} ({times})")
     log(f"N range {min(Ns)}..{max(Ns)}, mean {sum(Ns) / len(Ns):.0f}")
 
     def barrier():
@@ -408,7 +416,7 @@ def run_ours(args):
                                     ("FP32 eigensolve refined to FP64 accuracy "
                                      f"({args.eig_refine} iteration(s))"
                                      if args.erpa == "refined" else "FP64 dsyevd")),
-                           "streams": args.nstreams,
+                           "streams": args.nstreams, "streams_autotune": tuned,
                            "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens
                                          else "off"),
                            "eig_emulation": bool(args.eig_emulation),

@@ -363,6 +363,31 @@ def ac_energy_batched(batch: BatchInputs, ngrid: int = 8, precision: str = "fp64
         return ecorr, ecas, wl, status, st
     return ecorr, ecas, wl, status
 
+def autotune_streams(batch: BatchInputs, candidates=(4, 8, 12, 16), sample: int = 16,
+                     points: int = 2, precision: str = "fp64tc5", erpa_mode: str = "refined",
+                     ctx: Context | None = None):
+    """Choose the worker-stream count of ac_energy_batched for a batch: one pass of
+    `points` lambda points over the `sample` largest systems per candidate (after
+    one untimed pass), timed on the device; returns (best, {candidate: seconds}).
+    The large systems set the step time, and concurrency between their library
+    eigensolves is what the stream count trades against memory."""
+    import time
+    ctx = ctx or default_context(torch.device(batch.device).index or 0)
+    nd = np.asarray(batch.ndimx())
+    sub = batch.subset(np.argsort(-nd, kind="stable")[:sample])
+    lams = np.linspace(0.1, 0.9, points)
+    kw = dict(lambdas=lams, precision=precision, erpa_mode=erpa_mode, ctx=ctx)
+    ac_energy_batched(sub, nstreams=candidates[0], **kw)
+    times = {}
+    for ns in candidates:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ac_energy_batched(sub, nstreams=int(ns), **kw)
+        torch.cuda.synchronize()
+        times[int(ns)] = time.perf_counter() - t0
+    return min(times, key=times.get), times
+
+
 class AcSession:
     """Batch with per-system device state kept between calls (gc_ac_session_*):
     points(idx, lambdas) evaluates W(lambda) for some systems, building a
