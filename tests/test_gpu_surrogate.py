@@ -64,3 +64,13 @@ def test_session_points_reuse_state_and_validate(gpu_lib):
             ses.points([1, 1], x8[:1])
         with pytest.raises(GcError):
             ses.points([4], x8[:1])
+
+
+def test_autotune_streams_picks_a_candidate(gpu_lib):
+    from gammcor_gb300 import api, synth
+    shapes = surrogate.shapes(3, seed=11, nmin=30, nmax=40)
+    systems = [synth.make_system_device(d["n"], d["nin"], d["nact"], d["rank"], d["seed"])
+               for d in shapes]
+    batch = api.BatchInputs(systems, "cuda:0")
+    best, times = api.autotune_streams(batch, candidates=(1, 2), sample=3, points=1)
+    assert best in (1, 2) and set(times) == {1, 2} and all(t > 0 for t in times.values())
