@@ -28,7 +28,7 @@ enum gc_status {
   GC_ENOTPD = 5,      /* Cholesky found A+B not positive definite */
   GC_ETIMEOUT = 6,    /* a bounded device wait ran out */
   GC_ENOMEM = 7,      /* device allocation failed */
-  GC_EUNSUPPORTED = 8 /* shape or mode this build does not handle */
+  GC_EUNSUPPORTED = 8 /* shape or mode the library does not handle */
 };
 
 /* Arithmetic of the integral transform and of the integrand contraction. */
