@@ -1,8 +1,8 @@
 """CPU FP64 restatement of GAMMCOR's AC-CAS (FOFO) path.
 
-TEST INFRASTRUCTURE ONLY. This module is the checker for the CUDA path: only
-tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import it.
-The product path never calls it.
+TEST INFRASTRUCTURE ONLY. This module is the oracle the CUDA path is checked
+against: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+reference legs may import it. The product path never calls it.
 
 Parity status: UNPINNED against reference-produced numbers. The reference is
 Fortran + MKL and cannot be compiled where this project is built (no Fortran
