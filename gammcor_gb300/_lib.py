@@ -13,7 +13,8 @@ LIB_PATH = _HERE / "libgammcor_gpu.so"
 
 GC_OK = 0
 STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "GC_ECUSOLVER",
-                5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED"}
+                5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED",
+                9: "GC_ENONFINITE"}
 PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "fp64tc5": 3, "fp64tc6": 4}
 ERPA = {"symm1": 0, "cholesky": 1, "refined": 2}
 
@@ -43,6 +44,7 @@ SIGNATURES = {
     "gc_set_eig_emulation": (C.c_int, [_vp, C.c_int]),
     "gc_set_eig_refinement": (C.c_int, [_vp, C.c_int]),
     "gc_set_chol_blocked": (C.c_int, [_vp, C.c_int]),
+    "gc_set_pipeline_wait": (C.c_int, [_vp, C.c_ulonglong]),
     "gc_eig_refine_stats": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]),
     "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),

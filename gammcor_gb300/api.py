@@ -65,6 +65,11 @@ class Context:
         """Blocked Cholesky of A+B with tensor-core trailing updates (N >= 1536)."""
         check(self.h, load().gc_set_chol_blocked(self.h, int(on)))
 
+    def set_pipeline_wait(self, ns: int):
+        """Limit of the tensor-core GEMMs' pipeline waits in ns (0: the 1 s default);
+        shortening it injects a timeout for tests."""
+        check(self.h, load().gc_set_pipeline_wait(self.h, int(ns)))
+
     def eig_refine_stats(self) -> dict:
         """Refined ERPA counters: solves, dsyevd fallbacks, largest block cluster."""
         s, f, m = C.c_longlong(), C.c_longlong(), C.c_int()
@@ -231,16 +236,26 @@ def ace_ne_erpa_fofo(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray, i
 def ace_ne_erpa_fofo_noalloc(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray,
                              indn: np.ndarray, nact: int, inactive: int, fofo: torch.Tensor,
                              ctx: Context | None = None) -> float:
-    """W(lambda) through the entry point that allocates no device memory (for
-    callers that cannot allocate; limits nbas <= 2048, NDimX <= 16384). evec
-    must already be a Fortran-layout (column-major) device matrix, e.g. the
-    view returned by erpasymm1, so that no copy is made here."""
+    """W(lambda) through the entry point that allocates no device memory, for
+    callers whose device memory belongs to their own pool or must not grow
+    (limits nbas <= 2048, NDimX <= 16384). Nothing is copied here: evec must
+    already be a Fortran-layout (column-major) FP64 device matrix, e.g. the view
+    returned by erpasymm1, and evals and fofo contiguous FP64 tensors on the
+    context's device."""
     ctx = ctx or default_context(fofo.device.index or 0)
     occ = np.ascontiguousarray(occ, dtype=np.float64)
     ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
     ycol = evec.t()
     if not ycol.is_contiguous():
         raise ValueError("evec must be column-major (a .t() view of a contiguous tensor)")
+    for name, x in (("evec", evec), ("evals", evals), ("fofo", fofo)):
+        if x.dtype != torch.float64:
+            raise ValueError(f"{name} must be float64, got {x.dtype}")
+        if not x.is_cuda or x.device.index != ctx.device:
+            raise ValueError(f"{name} must be on cuda:{ctx.device}, got {x.device}")
+    for name, x in (("evals", evals), ("fofo", fofo)):
+        if not x.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
     w = C.c_double()
     check(ctx.h, load().gc_ace_ne_erpa_fofo_noalloc(ctx.h, occ.shape[0], inactive, nact,
                                                     ind.shape[0] // 2, _dptr(occ), _iptr(ind),

@@ -55,7 +55,8 @@ int gc_create(gc_context **out, int device, void *stream) {
   }
   if (cudaMalloc(&ctx->dev_info, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->dev_flag, sizeof(int)) != cudaSuccess ||
-      cudaMemset(ctx->dev_flag, 0, sizeof(int)) != cudaSuccess) {
+      cudaMemset(ctx->dev_flag, 0, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->dev_nonfinite, sizeof(int)) != cudaSuccess) {
     gc_destroy(ctx);
     return GC_ENOMEM;
   }
@@ -70,6 +71,7 @@ int gc_destroy(gc_context *ctx) {
   if (ctx->cublas) cublasDestroy(ctx->cublas);
   if (ctx->dev_info) cudaFree(ctx->dev_info);
   if (ctx->dev_flag) cudaFree(ctx->dev_flag);
+  if (ctx->dev_nonfinite) cudaFree(ctx->dev_nonfinite);
   delete ctx;
   return GC_OK;
 }

@@ -10,6 +10,8 @@
 //   * the one-body part reads HNO, AuxI, AuxIO and WMAT (n x n), which the
 //     reference accumulates in the same loops.
 // Every coefficient is 1, lambda or (1 - lambda), so A+-B is affine in lambda.
+#include <cmath>
+
 #include "gc_internal.cuh"
 
 namespace {
@@ -433,6 +435,15 @@ int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int 
     return set_error(ctx, GC_EINVAL, "system: bad arguments nbas=%d ninact=%d nact=%d ndimx=%d",
                      nbas, ninact, nact, ndimx);
   const int n = nbas, nocc = ninact + nact;
+  auto finite = [](const double *x, size_t cnt) {
+    for (size_t i = 0; i < cnt; ++i)
+      if (!std::isfinite(x[i])) return false;
+    return true;
+  };
+  if (!finite(occ, n) || (xone && !finite(xone, (size_t)n * (n + 1) / 2)) ||
+      (nact > 0 && !finite(rdm2act, (size_t)nact * nact * (nact * nact + 1) / 2)))
+    return set_error(ctx, GC_ENONFINITE,
+                     "system: non-finite value in the occupations, one-electron integrals or 2-RDM");
   sd.n = n;
   sd.nin = ninact;
   sd.nact = nact;

@@ -267,7 +267,7 @@ extern "C" int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *
     if (status) status[i] = rr;
     return rr;
   };
-  r = run_tasks(ctx, ws, nsys, task, [&](int rr) { return status && rr == GC_ENOTPD; });
+  r = run_tasks(ctx, ws, nsys, task, [&](int rr) { return status && (rr == GC_ENOTPD || rr == GC_ENONFINITE); });
   free_workers(ws);
   return r;
 }
@@ -338,7 +338,7 @@ extern "C" int gc_ac_session_points(gc_ac_session *s, int nidx, const int *idx, 
     if (status) status[j] = rr;
     return rr;
   };
-  return run_tasks(ctx, s->ws, nidx, task, [&](int rr) { return status && rr == GC_ENOTPD; });
+  return run_tasks(ctx, s->ws, nidx, task, [&](int rr) { return status && (rr == GC_ENOTPD || rr == GC_ENONFINITE); });
 }
 
 extern "C" int gc_ac_session_destroy(gc_ac_session *s) {

@@ -92,6 +92,17 @@ __global__ void k_norm_chol(int N, double *__restrict__ Y, double *__restrict__ 
   if (i < N) Y[(size_t)nu * N + i] *= 1.0 / sqrt(2.0 * om);
 }
 
+// *count += number of non-finite elements of a and b (n elements each).
+__global__ void k_count_nonfinite(size_t n, const double *__restrict__ a,
+                                  const double *__restrict__ b, int *count) {
+  int c = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    c += !isfinite(a[i]) + !isfinite(b[i]);
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
 __global__ void k_sqrt_eig(int N, double *__restrict__ eig) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < N && eig[i] > kSmall) eig[i] = sqrt(eig[i]);
@@ -640,7 +651,7 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
   }
   int hflag[2] = {0, 0};
   GC_CUDA(ctx, cudaMemcpyAsync(hflag, flag.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  GC_TRY(gc::check_flag(ctx));  // synchronises; a refinement GEMM whose wait expired fails here
   ctx->refine_max_cluster = std::max(ctx->refine_max_cluster, hflag[1]);
   if (hflag[0] != 0) {
     *fallback = true;
@@ -718,7 +729,7 @@ int chol_blocked(gc_context *ctx, int N, double *A, int prec, int nb, int *minor
   std::vector<int> h(nblk);
   GC_CUDA(ctx, cudaMemcpyAsync(h.data(), infos.p, nblk * sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
-  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  GC_TRY(gc::check_flag(ctx));  // synchronises; covers the trailing-update GEMMs
   for (int blk = 0; blk < nblk; ++blk) {
     if (h[blk] < 0) return gc::set_error(ctx, GC_ECUSOLVER, "potrf info=%d", h[blk]);
     if (h[blk] > 0) {  // later blocks worked on an invalid update: report the first
@@ -751,13 +762,26 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
                int mode, int gemm_precision) {
   if (N <= 0 || !abplus || !abmin || !Y || !eig)
     return set_error(ctx, GC_EINVAL, "erpa: bad arguments N=%d", N);
+  const size_t NN = (size_t)N * N;
+  {
+    // No eigensolver is handed a matrix with a NaN or an infinity.
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->dev_nonfinite, 0, sizeof(int), ctx->stream));
+    const unsigned grid = std::min<size_t>(ceil_div(NN, 256), 152 * 8);
+    k_count_nonfinite<<<grid, 256, 0, ctx->stream>>>(NN, abplus, abmin, ctx->dev_nonfinite);
+    GC_LAUNCHED(ctx);
+    int bad = 0;
+    GC_CUDA(ctx, cudaMemcpyAsync(&bad, ctx->dev_nonfinite, sizeof(int), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (bad)
+      return set_error(ctx, GC_ENONFINITE, "erpa: %d non-finite elements in A+B / A-B", bad);
+  }
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
   k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abplus);
   GC_LAUNCHED(ctx);
   k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abmin);
   GC_LAUNCHED(ctx);
   const double one = 1.0, zero = 0.0;
-  const size_t NN = (size_t)N * N;
   if (mode == GC_ERPA_SYMM1) {
     DevBuf<double> V, P, H;
     GC_TRY(V.alloc(ctx, NN));
@@ -843,7 +867,8 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
 extern "C" int gc_erpa(gc_context *ctx, int ndimx, double *abplus, double *abmin, double *eigvec,
                        double *eig, int mode) {
   if (!ctx) return GC_EINVAL;
-  return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, GC_PREC_FP64);
+  GC_TRY(gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, GC_PREC_FP64));
+  return gc::check_flag(ctx);  // the refined form's BF16 product of E E^T runs on tensor cores
 }
 
 extern "C" int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus, double *abmin,
@@ -851,7 +876,16 @@ extern "C" int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus, double *ab
   if (!ctx) return GC_EINVAL;
   if (precision != GC_PREC_FP64 && precision != GC_PREC_FP64TC5 && precision != GC_PREC_FP64TC6)
     return gc::set_error(ctx, GC_EINVAL, "gc_erpa_ex: precision %d is not FP64-accurate", precision);
-  return gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, precision);
+  GC_TRY(gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, precision));
+  return gc::check_flag(ctx);
+}
+
+extern "C" int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns) {
+  if (!ctx) return GC_EINVAL;
+  if (ns > 1000000000ull)
+    return gc::set_error(ctx, GC_EINVAL, "pipeline wait limit %llu ns above 1 s", ns);
+  ctx->wait_ns = ns ? ns : 1000000000ull;
+  return GC_OK;
 }
 
 extern "C" int gc_set_eig_refinement(gc_context *ctx, int iterations) {

@@ -9,6 +9,8 @@
 // replace N^2 dot products of length N. On the tensor-core path the diagonal of
 // Kt is taken out of the product and its term 2 Kt_ii (Yk Yk^T)_ii, which
 // nearly cancels the diagonal correction, is summed in FP64.
+#include <cmath>
+
 #include "gc_internal.cuh"
 #include "gc_tc_gemm.cuh"
 
@@ -125,6 +127,8 @@ int integrand(gc_context *ctx, const SysDev &sd, const double *Y, const double *
     double dsum = 0.0;
     for (double v : hd) dsum += v;
     *w_host = 2.0 * dot + dsum;
+    if (!std::isfinite(*w_host))
+      return set_error(ctx, GC_ENONFINITE, "integrand: W is not finite (non-finite integrals?)");
     return GC_OK;
   }
   k_contract<<<nb, 256, 0, ctx->stream>>>(NN, N, yk.p, t.p, diag.p, part.p);
@@ -135,6 +139,8 @@ int integrand(gc_context *ctx, const SysDev &sd, const double *Y, const double *
   double w = 0.0;
   for (int b = 0; b < nb; ++b) w += hp[b];
   *w_host = w;
+  if (!std::isfinite(w))
+    return set_error(ctx, GC_ENONFINITE, "integrand: W is not finite (non-finite integrals?)");
   return GC_OK;
 }
 

@@ -20,6 +20,7 @@ struct gc_context {
   cusolverDnHandle_t cusolver = nullptr;
   int *dev_info = nullptr;           // cuSOLVER info slot
   int *dev_flag = nullptr;           // device error flag for bounded waits
+  int *dev_nonfinite = nullptr;      // count of non-finite matrix elements (ERPA input check)
   long long launches = 0;            // kernels of this library launched
   int eig_emulation = 0;             // cuSOLVER FP64 emulation strategy EAGER when 1
   int eig_refine = 2;                // refinement iterations of the FP32 eigensolve
@@ -27,6 +28,7 @@ struct gc_context {
   long long refine_fallbacks = 0;    // of which fell back to dsyevd
   int refine_max_cluster = 0;        // largest cluster diagonalised in a block
   int chol_blocked = 1;              // blocked Cholesky with tensor-core trailing updates
+  unsigned long long wait_ns = 1000000000ull;  // limit of the tensor-core GEMMs' pipeline waits
   std::string err;
 };
 

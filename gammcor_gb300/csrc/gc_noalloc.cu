@@ -2,17 +2,19 @@
 //
 // Some hosts of this library cannot call cudaMalloc at the point where they
 // need the integrand: a Fortran program whose device memory is owned by its
-// own pool, code running while a CUDA graph is being captured, or a process
-// that must not grow its device footprint after start-up. For them this file
-// provides gc_ace_ne_erpa_fofo_noalloc, a variant of the integrand that works
-// only in a fixed, file-scope device array and in the buffers the caller
-// passes (eigenvectors, eigenvalues, FOFO integrals).
+// own pool, or a process that must not grow its device footprint after
+// start-up. For them this file provides gc_ace_ne_erpa_fofo_noalloc, a variant
+// of the integrand that works only in a fixed, file-scope device array and in
+// the buffers the caller passes (eigenvectors, eigenvalues, FOFO integrals).
 //
 // The variant fuses what gc_ace_ne_erpa_fofo stages in N x N scratch
 // matrices: each block builds tiles of S = Yk Yk^T from the eigenvectors
 // (kept modes only), multiplies them with the masked, CI-weighted FOFO
 // integrals gathered on the fly and leaves one partial sum; a one-block kernel
-// adds the partials. FP64 throughout.
+// adds the partials. The summand is symmetric in the two pairs, so only tiles
+// on or above the diagonal are formed and the off-diagonal ones count twice:
+// about N^3 FP64 multiply-adds per call (a few seconds at the NDimX limit).
+// FP64 throughout.
 #include <mutex>
 
 #include "gc_internal.cuh"
@@ -31,6 +33,7 @@ constexpr size_t kOffOcc = kOffIndn + sizeof(int) * 2 * kMaxPairs;
 constexpr size_t kOffPart = kOffOcc + sizeof(double) * kMaxBasis;
 constexpr size_t kOffRes = kOffPart + sizeof(double) * kBlocks;
 constexpr size_t kScratchBytes = kOffRes + 256;
+static_assert(kScratchBytes == 155904, "the array size stated in include/gammcor_gpu.h");
 
 // Shared by every call on a device; it keeps the last call's contents.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -51,12 +54,18 @@ __global__ void k_integrand_tiles(int n, int nin, int nocc, int N, const double 
   __shared__ double yi[kTile][kTile + 1], yj[kTile][kTile + 1];
   __shared__ double red[kTile * kTile];
   const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
-  const int tiles = (N + kTile - 1) / kTile;
-  const long long ntiles = (long long)tiles * tiles;
+  const long long tiles = (N + kTile - 1) / kTile;
+  const long long ntiles = tiles * (tiles + 1) / 2;  // tiles (ti, tj) with ti <= tj
   const size_t ld = (size_t)n * nocc;
   double acc = 0.0;
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int i0 = (int)(t % tiles) * kTile, j0 = (int)(t / tiles) * kTile;
+    // t = tj (tj + 1) / 2 + ti, 0 <= ti <= tj
+    long long tj = (long long)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (tj * (tj + 1) / 2 > t) --tj;
+    while ((tj + 1) * (tj + 2) / 2 <= t) ++tj;
+    const long long ti = t - tj * (tj + 1) / 2;
+    const int i0 = (int)ti * kTile, j0 = (int)tj * kTile;
+    const double wt = ti == tj ? 1.0 : 2.0;  // off-diagonal tiles stand for their mirror too
     const int i = i0 + tx, j = j0 + ty;
     double s = 0.0;
     for (int v0 = 0; v0 < N; v0 += kTile) {
@@ -83,7 +92,7 @@ __global__ void k_integrand_tiles(int n, int nin, int nocc, int N, const double 
         double c = (cicoef(occ[p]) + cicoef(occ[q])) * (cicoef(occ[r]) + cicoef(occ[u]));
         double a = 2.0 * c * s;
         if (i == j) a -= occ[p] * (1.0 - occ[q]) + occ[q] * (1.0 - occ[p]);
-        acc += a * f;
+        acc += wt * a * f;
       }
     }
   }
@@ -156,14 +165,21 @@ extern "C" int gc_ace_ne_erpa_fofo_noalloc(gc_context *ctx, int nbas, int ninact
       return gc::set_error(ctx, GC_EINVAL, "noalloc integrand: pair %d = (%d,%d) is not valid",
                            i + 1, a + 1, b + 1);
   }
+  // The array's address is per device: the call runs on the context's device only.
+  int cur = -1;
+  GC_CUDA(ctx, cudaGetDevice(&cur));
+  if (cur != ctx->device)
+    return gc::set_error(ctx, GC_EINVAL,
+                         "noalloc integrand: current device %d is not the context's device %d", cur,
+                         ctx->device);
   unsigned char *scr = nullptr;
   GC_TRY(scratch_address(ctx, &scr));
   GC_CUDA(ctx, cudaMemcpyAsync(scr + kOffIndn, indn_host, sizeof(int) * 2 * ndimx,
                                cudaMemcpyHostToDevice, ctx->stream));
   GC_CUDA(ctx, cudaMemcpyAsync(scr + kOffOcc, occ_host, sizeof(double) * nbas,
                                cudaMemcpyHostToDevice, ctx->stream));
-  const long long tiles = (long long)((ndimx + kTile - 1) / kTile) * ((ndimx + kTile - 1) / kTile);
-  const int nb = (int)std::min<long long>(kBlocks, tiles);
+  const long long tn = (ndimx + kTile - 1) / kTile;
+  const int nb = (int)std::min<long long>(kBlocks, tn * (tn + 1) / 2);
   k_integrand_tiles<<<nb, kTile * kTile, 0, ctx->stream>>>(nbas, ninact, nocc, ndimx, eigvec_dev,
                                                             eig_dev, fofo_dev, scr);
   GC_LAUNCHED(ctx);

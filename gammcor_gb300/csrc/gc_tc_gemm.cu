@@ -15,8 +15,11 @@
 //           (M=128, N=BN, K=16) and tcgen05.commit to release ring slots;
 //   warps 2-5 epilogue: tcgen05.ld of the accumulator, then either a FP64
 //           store or a fused dot product with an FP64 matrix (integrand).
-// Every mbarrier wait is bounded; on expiry the CTA records an error in a
-// device flag, drains its own copies and frees TMEM before returning.
+// Every pipeline wait is bounded by the context's limit (1 s unless a test
+// shortens it). On expiry the CTA records an error in a device flag and stops
+// issuing work; before it frees TMEM and exits, the producer waits for the TMA
+// copies it issued and the MMA thread commits the MMAs it issued and waits for
+// them, both under their own fixed 1 s limit.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -30,7 +33,7 @@ constexpr int BM = 128;
 constexpr int BK = 64;  // bf16 elements per K slice = one 128-byte swizzle row
 constexpr int STAGES = 4;
 constexpr int MAXPASS = 8;
-constexpr unsigned long long kWaitNs = 1000000000ull;  // a wait longer than 1 s is an error
+constexpr unsigned long long kDrainNs = 1000000000ull;  // limit of the waits of the abort path
 
 struct PassList {
   int n;
@@ -68,8 +71,9 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-// Bounded parity wait: returns false if the phase did not complete within kWaitNs.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded parity wait: returns false if the phase did not complete within limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit_ns) {
   uint32_t addr = smem_u32(bar);
   unsigned long long t0 = 0;
   for (unsigned it = 0;; ++it) {
@@ -85,7 +89,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     if ((it & 255) == 0) {
       unsigned long long t = globaltimer();
       if (t0 == 0) t0 = t;
-      else if (t - t0 > kWaitNs) return false;
+      else if (t - t0 > limit_ns) return false;
     }
   }
 }
@@ -177,7 +181,7 @@ template <int BN>
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
               int M, int N, int kblocks, int a_batched, int b_batched, PassList passes, Epi epi,
-              int *err_flag) {
+              int *err_flag, unsigned long long wait_ns) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
@@ -188,6 +192,7 @@ __global__ void __launch_bounds__(192, 1)
   uint64_t *accf = empty + STAGES;
   uint32_t *tmem_slot = (uint32_t *)(accf + 1);
   __shared__ int abort_flag;
+  volatile int *abort_v = &abort_flag;
   __shared__ double red[4];
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -220,11 +225,11 @@ __global__ void __launch_bounds__(192, 1)
     for (int it = 0; it < total; ++it) {
       int s = it % STAGES;
       uint32_t ph = (it / STAGES) & 1;
-      if (!mbar_wait(&empty[s], ph ^ 1)) {
+      if (!mbar_wait(&empty[s], ph ^ 1, wait_ns)) {
         atomicExch(&abort_flag, 1);
         break;
       }
-      if (abort_flag) break;
+      if (*abort_v) break;
       int pass = it / kblocks, kb = it % kblocks;
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
       tma_load_4d(sA + s * A_BYTES, &mapA, &full[s], kb * BK, m0, a_batched ? b : 0,
@@ -233,10 +238,12 @@ __global__ void __launch_bounds__(192, 1)
                   passes.pb[pass]);
       issued = it + 1;
     }
-    if (abort_flag) {
-      // drain copies already issued into the ring before the CTA exits
+    if (*abort_v) {
+      // Drain the copies already issued into the ring before the CTA exits. Loads older
+      // than the last STAGES were consumed by the MMA thread (their slot was released
+      // before it was reused), so only the last STAGES can still be in flight.
       for (int it = (issued > STAGES ? issued - STAGES : 0); it < issued; ++it)
-        mbar_wait(&full[it % STAGES], (it / STAGES) & 1);
+        mbar_wait(&full[it % STAGES], (it / STAGES) & 1, kDrainNs);
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
@@ -245,7 +252,7 @@ __global__ void __launch_bounds__(192, 1)
     for (int it = 0; it < total && ok; ++it) {
       int s = it % STAGES;
       uint32_t ph = (it / STAGES) & 1;
-      if (!mbar_wait(&full[s], ph) || abort_flag) {
+      if (!mbar_wait(&full[s], ph, wait_ns) || *abort_v) {
         atomicExch(&abort_flag, 1);
         ok = false;
         break;
@@ -260,14 +267,17 @@ __global__ void __launch_bounds__(192, 1)
       mma_commit(&empty[s]);
     }
     mma_commit(accf);  // arrives once all issued MMAs have completed
+    // TMEM is freed after the final barrier: wait here for every MMA this thread
+    // issued, whatever the epilogue saw (on the abort path it may have given up).
+    if (!mbar_wait(accf, 0, kDrainNs)) atomicExch(&abort_flag, 1);
   } else if (warp >= 2) {
     // ---------------- epilogue
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int m = m0 + q * 32 + lane;
-    bool ok = mbar_wait(accf, 0);
+    bool ok = mbar_wait(accf, 0, wait_ns);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     double acc = 0.0;
-    if (ok && !abort_flag) {
+    if (ok && !*abort_v) {
       for (int c0 = 0; c0 < BN; c0 += 16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
@@ -319,6 +329,11 @@ constexpr int OZ_BN = 64;
 constexpr int OZ_BK = 32;      // K per stage: 32 BF16 = one 64-byte swizzled row
 constexpr int OZ_STAGES = 3;   // each stage holds every slice of A and of B
 constexpr int OZ_MAXS = 6;
+// Row exponent of a row holding a NaN or an infinity: its slices are zero and
+// every product element of the row comes out NaN, so non-finite inputs stay
+// visible in the result (the integer slices cannot carry them).
+constexpr int kBadExp = 0x7fffffff;
+
 constexpr int OZ_EPI_WARPS = 8;                   // two per TMEM lane quarter
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;  // TMA warp, MMA warp, epilogue
 
@@ -347,7 +362,7 @@ template <int S>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_tc_gemm_oz(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  int M, int N, int kblocks, int a_batched, int b_batched, OzPlan plan, OzEpi epi,
-                 int *err_flag) {
+                 int *err_flag, unsigned long long wait_ns) {
   // One stage = the K block [kb*32, kb*32+32) of all S slices of the A tile (128 rows)
   // and of the B tile (OZ_BN rows): every slice product t+u < S of the block is
   // issued from it, so each slice tile crosses L2 -> shared memory once per block.
@@ -359,8 +374,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   uint64_t *empty = full + OZ_STAGES;
   uint64_t *accf = empty + OZ_STAGES;
   uint64_t *acce = accf + 1;
-  uint32_t *tmem_slot = (uint32_t *)(acce + 1);
+  uint64_t *drainb = acce + 1;  // abort path: completion of the MMAs already issued
+  uint32_t *tmem_slot = (uint32_t *)(drainb + 1);
   __shared__ int abort_flag;
+  volatile int *abort_v = &abort_flag;
   __shared__ double red[OZ_EPI_WARPS];
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
@@ -378,6 +395,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     }
     mbar_init(accf, 1);
     mbar_init(acce, OZ_EPI_WARPS);
+    mbar_init(drainb, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -394,9 +412,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
 
   if (warp == 0 && lane == 0) {
     int issued = 0;
-    for (int kb = 0; kb < kblocks && !abort_flag; ++kb) {
+    for (int kb = 0; kb < kblocks && !*abort_v; ++kb) {
       const int s = kb % OZ_STAGES;
-      if (!mbar_wait(&empty[s], ((kb / OZ_STAGES) & 1) ^ 1)) {
+      if (!mbar_wait(&empty[s], ((kb / OZ_STAGES) & 1) ^ 1, wait_ns)) {
         atomicExch(&abort_flag, 1);
         break;
       }
@@ -411,14 +429,14 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                     b_batched ? b : 0, u);
       issued = kb + 1;
     }
-    if (abort_flag)
+    if (*abort_v)  // only the last OZ_STAGES loads can still be in flight
       for (int j = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); j < issued; ++j)
-        mbar_wait(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1);
+        mbar_wait(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1, kDrainNs);
   } else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = instr_desc(OZ_BN);
     bool ok = true;
     for (int g = 0; g < nchunks && ok; ++g) {
-      if (g > 0 && !mbar_wait(acce, (g - 1) & 1)) {
+      if (g > 0 && !mbar_wait(acce, (g - 1) & 1, wait_ns)) {
         ok = false;
         break;
       }
@@ -426,7 +444,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int kb0 = g * plan.chunk_kb, kb1 = min(kblocks, kb0 + plan.chunk_kb);
       for (int kb = kb0; kb < kb1; ++kb) {
         const int s = kb % OZ_STAGES;
-        if (!mbar_wait(&full[s], (kb / OZ_STAGES) & 1) || abort_flag) {
+        if (!mbar_wait(&full[s], (kb / OZ_STAGES) & 1, wait_ns) || *abort_v) {
           ok = false;
           break;
         }
@@ -449,6 +467,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       mma_commit(accf);
     }
     if (!ok) atomicExch(&abort_flag, 1);
+    // TMEM is freed after the final barrier, and the epilogue may have given up on the
+    // last chunk: commit every MMA issued so far (a chunk may be half issued) to a
+    // barrier of its own and wait until they have completed.
+    mma_commit(drainb);
+    if (!mbar_wait(drainb, 0, kDrainNs)) atomicExch(&abort_flag, 1);
   } else if (warp >= 2) {
     // Every chunk's FP32 sums are integers below 2^24, so the weights fold into one
     // int64 per column by Horner in base 2^7: t = sum_d v_d 2^(7 (SI - 1 - d)) is exact
@@ -467,7 +490,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     for (int j = 0; j < NC; ++j) acc[j] = 0;
     bool ok = true;
     for (int g = 0; g < nchunks && ok; ++g) {
-      if (!mbar_wait(accf, g & 1) || abort_flag) {
+      if (!mbar_wait(accf, g & 1, wait_ns) || *abort_v) {
         ok = false;
         break;
       }
@@ -498,12 +521,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (!ok) atomicExch(&abort_flag, 1);
     double dot = 0.0;
     if (ok && m < M) {
-      const int er = epi.ea[(long long)b * epi.ea_sb + m] - 7 * (SI + 1);
+      const int ea = epi.ea[(long long)b * epi.ea_sb + m];
+      const int er = ea - 7 * (SI + 1);
 #pragma unroll
       for (int j = 0; j < NC; ++j) {
         int n = n0 + h * NC + j;
         if (n < N) {
-          double cv = ldexp((double)acc[j], er + epi.eb[(long long)b * epi.eb_sb + n]);
+          const int eb = epi.eb[(long long)b * epi.eb_sb + n];
+          double cv = (ea == kBadExp || eb == kBadExp) ? __longlong_as_double(0x7ff8000000000000ll)
+                                                       : ldexp((double)acc[j], er + eb);
           long long o = (long long)b * epi.sb + m + (long long)n * epi.ldn;
           if (epi.mode == 0)
             epi.c[o] = cv;
@@ -532,7 +558,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   }
 }
 
-// Row exponents: e[b][r] = 1 + ilogb(max_k |x[b,r,k]|) (0 for a zero row).
+// Row exponents: e[b][r] = 1 + ilogb(max_k |x[b,r,k]|) (0 for a zero row,
+// kBadExp for a row with a non-finite element).
 __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, int nb, long long sr,
                                long long sk, long long sb, int *__restrict__ e) {
   long long total = (long long)nb * rows;
@@ -544,9 +571,15 @@ __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, in
     long long bb = t / rows;
     const double *row = x + bb * sb + (long long)r * sr;
     double mx = 0.0;
-    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(row[(long long)k * sk]));
+    bool bad = false;
+    for (int k = lane; k < K; k += 32) {
+      const double v = row[(long long)k * sk];
+      bad |= !isfinite(v);
+      mx = fmax(mx, fabs(v));
+    }
     for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
-    if (lane == 0) e[t] = mx > 0.0 ? ilogb(mx) + 1 : 0;
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane == 0) e[t] = bad ? kBadExp : (mx > 0.0 ? ilogb(mx) + 1 : 0);
   }
 }
 
@@ -556,7 +589,7 @@ __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, in
 // (the FP64 pipe is the narrow one on this part).
 __device__ __forceinline__ void store_digits(double x, int e, int S, long long plane, long long o,
                                              __nv_bfloat16 *__restrict__ planes) {
-  long long n = __double2ll_rn(ldexp(x, 7 * S - e));
+  long long n = e == kBadExp ? 0 : __double2ll_rn(ldexp(x, 7 * S - e));
   for (int s = S - 1; s > 0; --s) {
     const long long d = ((n + 64) & 127) - 64;
     planes[s * plane + o] = __float2bfloat16_rn((float)d);
@@ -744,21 +777,12 @@ int run_gemm(gc_context *ctx, const Operand &A, const Operand &B, int M, int N, 
   GC_CUDA(ctx, cfg);
   dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, BN_T), nbatch);
   k_tc_gemm<BN_T><<<grid, 192, smem_bytes(BN_T), ctx->stream>>>(
-      A.map, B.map, M, N, A.Kp / BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag);
+      A.map, B.map, M, N, A.Kp / BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag,
+      ctx->wait_ns);
   GC_LAUNCHED(ctx);
   return GC_OK;
 }
 
-int check_flag(gc_context *ctx) {
-  int flag = 0;
-  GC_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->dev_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  if (flag) {
-    cudaMemsetAsync(ctx->dev_flag, 0, sizeof(int), ctx->stream);
-    return gc::set_error(ctx, GC_ETIMEOUT, "tc_gemm: a bounded mbarrier wait expired");
-  }
-  return GC_OK;
-}
 
 
 // ---- sliced (FP64-accurate) operands and launch
@@ -829,9 +853,9 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
   return GC_OK;
 }
 
-size_t oz_smem_bytes(int S) {
+size_t oz_smem_bytes(int S) {  // alignment pad, stages, 2 * stages + 3 barriers, TMEM slot
   return 1024 + OZ_STAGES * (size_t)S * (BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) +
-         (2 * OZ_STAGES + 2) * 8 + 16;
+         (2 * OZ_STAGES + 3) * 8 + 16;
 }
 
 template <int S>
@@ -846,7 +870,8 @@ int launch_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, in
   GC_CUDA(ctx, cfg);
   dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, OZ_BN), nbatch);
   k_tc_gemm_oz<S><<<grid, OZ_THREADS, oz_smem_bytes(S), ctx->stream>>>(
-      A.map, B.map, M, N, A.Kp / OZ_BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag);
+      A.map, B.map, M, N, A.Kp / OZ_BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag,
+      ctx->wait_ns);
   GC_LAUNCHED(ctx);
   return GC_OK;
 }
@@ -865,6 +890,17 @@ int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N
 }  // namespace
 
 namespace gc {
+
+int check_flag(gc_context *ctx) {
+  int flag = 0;
+  GC_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->dev_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag) {
+    GC_CUDA(ctx, cudaMemsetAsync(ctx->dev_flag, 0, sizeof(int), ctx->stream));
+    return gc::set_error(ctx, GC_ETIMEOUT, "tc_gemm: a bounded mbarrier wait expired");
+  }
+  return GC_OK;
+}
 
 int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M, int nX,
                  const double *CX, int nY, const double *CY, double *T1, double *out,
@@ -887,7 +923,7 @@ int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M
       OzEpi e{0, out, nX, ostride, nullptr, nullptr, nullptr, nullptr, 0, 0};
       GC_TRY(run_oz(ctx, A, B, nX, nY, cnt, pl, e));
     }
-    return check_flag(ctx);
+    return GC_OK;  // the device flag is read at the caller's next sync point
   }
   int S;
   PassList pl = pass_list(precision, &S);
@@ -908,7 +944,7 @@ int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M
     Epi e{0, out, nX, ostride, nullptr, nullptr};
     GC_TRY(run_gemm(ctx, A, B, nX, nY, cnt, pl, e));
   }
-  return check_flag(ctx);
+  return GC_OK;  // the device flag is read at the caller's next sync point
 }
 
 int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double *A, int lda,
@@ -926,7 +962,7 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
     GC_TRY(make_oz_operand(ctx, b, B, n, k, 1, 1, ldb, 0, pl.S, OZ_BN));
     OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
     GC_TRY(run_oz(ctx, a, b, m, n, 1, pl, e));
-    return check_flag(ctx);
+    return GC_OK;  // the device flag is read at the caller's next sync point
   }
   int S;
   PassList pl = pass_list(precision, &S);
@@ -936,7 +972,7 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
   GC_TRY(make_operand(ctx, b, B, n, k, 1, 1, ldb, 0, S, BN_T));
   Epi e{0, C, ldc, 0, nullptr, nullptr};
   GC_TRY(run_gemm(ctx, a, b, m, n, 1, pl, e));
-  return check_flag(ctx);
+  return GC_OK;  // the device flag is read at the caller's next sync point
 }
 
 int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const double *A,
@@ -950,7 +986,7 @@ int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const d
   GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
-  return check_flag(ctx);
+  return GC_OK;  // the device flag is read at the caller's next sync point
 }
 
 int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, const double *A,
@@ -964,7 +1000,7 @@ int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, c
   GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, period};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
-  return check_flag(ctx);
+  return GC_OK;  // the device flag is read at the caller's next sync point
 }
 
 int tc_dot_gemm(gc_context *ctx, int precision, int N, const double *Ksym, const double *Y,
@@ -1016,8 +1052,33 @@ extern "C" int gc_tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k
   if (!ctx) return GC_EINVAL;
   if (m <= 0 || n <= 0 || k <= 0 || lda < m || ldb < n || ldc < m || !A || !B || !C)
     return gc::set_error(ctx, GC_EINVAL, "tc_gemm_nt: bad arguments");
-  return gc::tc_gemm_nt(ctx, precision, m, n, k, A, lda, B, ldb, C, ldc);
+  GC_TRY(gc::tc_gemm_nt(ctx, precision, m, n, k, A, lda, B, ldb, C, ldc));
+  return gc::check_flag(ctx);
 }
+
+// Deterministic operands for gc_tc_gemm_time: x = u 2^-k with u uniform in
+// [-1, 1) and k in 0..19 from a hash of the element index, so that every row
+// mixes magnitudes over six decades (what the slicing sees on real operands).
+__global__ void k_fill_mixed(size_t n, unsigned long long seed, double *__restrict__ x) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long h = (i + 1) * 0x9E3779B97F4A7C15ull ^ seed;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    const double u = (double)(h >> 11) * 0x1.0p-53 * 2.0 - 1.0;
+    x[i] = ldexp(u, -(int)((h >> 3) % 20));
+  }
+}
+
+// CUDA event pair destroyed on every return path.
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
 
 extern "C" int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int k, int reps,
                                double *ms_per_launch) {
@@ -1025,57 +1086,44 @@ extern "C" int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int
   if (m <= 0 || n <= 0 || k <= 0 || reps <= 0 || !ms_per_launch ||
       (precision != GC_PREC_BF16X3 && precision != GC_PREC_BF16X6 && !is_oz(precision)))
     return gc::set_error(ctx, GC_EINVAL, "tc_gemm_time: bad arguments");
-  if (is_oz(precision)) {
-    OzPlan pl = oz_plan(precision);
-    gc::DevBuf<double> a, b, c;
-    GC_TRY(a.alloc(ctx, (size_t)m * k));
-    GC_TRY(b.alloc(ctx, (size_t)n * k));
-    GC_TRY(c.alloc(ctx, (size_t)m * n));
-    GC_CUDA(ctx, cudaMemsetAsync(a.p, 0, (size_t)m * k * 8, ctx->stream));
-    GC_CUDA(ctx, cudaMemsetAsync(b.p, 0, (size_t)n * k * 8, ctx->stream));
-    OzOperand A, B;
-    GC_TRY(make_oz_operand(ctx, A, a.p, m, k, 1, k, 1, 0, pl.S, BM));
-    GC_TRY(make_oz_operand(ctx, B, b.p, n, k, 1, k, 1, 0, pl.S, OZ_BN));
-    OzEpi e{0, c.p, m, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
-    GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));
-    cudaEvent_t t0, t1;
-    GC_CUDA(ctx, cudaEventCreate(&t0));
-    GC_CUDA(ctx, cudaEventCreate(&t1));
-    GC_CUDA(ctx, cudaEventRecord(t0, ctx->stream));
-    for (int r = 0; r < reps; ++r) GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));
-    GC_CUDA(ctx, cudaEventRecord(t1, ctx->stream));
-    GC_CUDA(ctx, cudaEventSynchronize(t1));
-    float ms = 0.f;
-    GC_CUDA(ctx, cudaEventElapsedTime(&ms, t0, t1));
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    *ms_per_launch = ms / reps;
-    return check_flag(ctx);
-  }
-  int S;
-  PassList pl = pass_list(precision, &S);
   gc::DevBuf<double> a, b, c;
   GC_TRY(a.alloc(ctx, (size_t)m * k));
   GC_TRY(b.alloc(ctx, (size_t)n * k));
   GC_TRY(c.alloc(ctx, (size_t)m * n));
-  GC_CUDA(ctx, cudaMemsetAsync(a.p, 0, (size_t)m * k * 8, ctx->stream));
-  GC_CUDA(ctx, cudaMemsetAsync(b.p, 0, (size_t)n * k * 8, ctx->stream));
-  Operand A, B;
-  GC_TRY(make_operand(ctx, A, a.p, m, k, 1, k, 1, 0, S, BM));
-  GC_TRY(make_operand(ctx, B, b.p, n, k, 1, k, 1, 0, S, BN_T));
-  Epi e{0, c.p, m, 0, nullptr, nullptr};
-  GC_TRY(run_gemm(ctx, A, B, m, n, 1, pl, e));  // warm-up
-  cudaEvent_t t0, t1;
-  GC_CUDA(ctx, cudaEventCreate(&t0));
-  GC_CUDA(ctx, cudaEventCreate(&t1));
-  GC_CUDA(ctx, cudaEventRecord(t0, ctx->stream));
-  for (int r = 0; r < reps; ++r) GC_TRY(run_gemm(ctx, A, B, m, n, 1, pl, e));
-  GC_CUDA(ctx, cudaEventRecord(t1, ctx->stream));
-  GC_CUDA(ctx, cudaEventSynchronize(t1));
+  k_fill_mixed<<<152 * 8, 256, 0, ctx->stream>>>((size_t)m * k, 0x1234567ull, a.p);
+  GC_LAUNCHED(ctx);
+  k_fill_mixed<<<152 * 8, 256, 0, ctx->stream>>>((size_t)n * k, 0x7654321ull, b.p);
+  GC_LAUNCHED(ctx);
+  EventPair ev;
+  GC_CUDA(ctx, cudaEventCreate(&ev.a));
+  GC_CUDA(ctx, cudaEventCreate(&ev.b));
   float ms = 0.f;
-  GC_CUDA(ctx, cudaEventElapsedTime(&ms, t0, t1));
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
+  if (is_oz(precision)) {
+    OzPlan pl = oz_plan(precision);
+    OzOperand A, B;
+    GC_TRY(make_oz_operand(ctx, A, a.p, m, k, 1, k, 1, 0, pl.S, BM));
+    GC_TRY(make_oz_operand(ctx, B, b.p, n, k, 1, k, 1, 0, pl.S, OZ_BN));
+    OzEpi e{0, c.p, m, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
+    GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));  // warm-up
+    GC_CUDA(ctx, cudaEventRecord(ev.a, ctx->stream));
+    for (int r = 0; r < reps; ++r) GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));
+    GC_CUDA(ctx, cudaEventRecord(ev.b, ctx->stream));
+    GC_CUDA(ctx, cudaEventSynchronize(ev.b));
+    GC_CUDA(ctx, cudaEventElapsedTime(&ms, ev.a, ev.b));
+  } else {
+    int S;
+    PassList pl = pass_list(precision, &S);
+    Operand A, B;
+    GC_TRY(make_operand(ctx, A, a.p, m, k, 1, k, 1, 0, S, BM));
+    GC_TRY(make_operand(ctx, B, b.p, n, k, 1, k, 1, 0, S, BN_T));
+    Epi e{0, c.p, m, 0, nullptr, nullptr};
+    GC_TRY(run_gemm(ctx, A, B, m, n, 1, pl, e));  // warm-up
+    GC_CUDA(ctx, cudaEventRecord(ev.a, ctx->stream));
+    for (int r = 0; r < reps; ++r) GC_TRY(run_gemm(ctx, A, B, m, n, 1, pl, e));
+    GC_CUDA(ctx, cudaEventRecord(ev.b, ctx->stream));
+    GC_CUDA(ctx, cudaEventSynchronize(ev.b));
+    GC_CUDA(ctx, cudaEventElapsedTime(&ms, ev.a, ev.b));
+  }
   *ms_per_launch = ms / reps;
-  return check_flag(ctx);
+  return gc::check_flag(ctx);
 }

@@ -6,6 +6,12 @@
 
 namespace gc {
 
+// Reads and clears the context's device flag (a bounded wait of a tensor-core
+// GEMM expired): GC_ETIMEOUT if it was set. Synchronises the context's stream.
+// The GEMM wrappers below do not synchronise; their callers read the flag at
+// their next synchronisation point.
+int check_flag(gc_context *ctx);
+
 // out_k (nX x nY, column-major, stride ostride) = CX^T M_k CY for cnt
 // column-major n x n matrices M_k; T1 is scratch of cnt*n*max(nX) doubles.
 int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M, int nX,

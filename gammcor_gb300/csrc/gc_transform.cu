@@ -141,7 +141,7 @@ extern "C" int gc_tran4_gen(gc_context *ctx, int nbas, int nA, const double *CA,
     GC_LAUNCHED(ctx);
     GC_TRY(gc::tc_two_sided(ctx, precision, n, cnt, M.p, nC, CC, nD, CD, T1.p, out + c0 * nCD, nCD));
   }
-  return GC_OK;
+  return precision == GC_PREC_FP64 ? GC_OK : gc::check_flag(ctx);
 }
 
 extern "C" int gc_tran4_factored(gc_context *ctx, int nbas, int rank, const double *L, int nA,
@@ -175,7 +175,7 @@ extern "C" int gc_tran4_factored(gc_context *ctx, int nbas, int rank, const doub
   const double *Zp = same ? Y.p : Z.p;
   GC_TRY(gc::tc_gemm_nt(ctx, precision, (int)nCD, (int)nAB, rank, Zp, (int)nCD, Y.p, (int)nAB, out,
                         (int)nCD));
-  return GC_OK;
+  return precision == GC_PREC_FP64 ? GC_OK : gc::check_flag(ctx);
 }
 
 namespace gc {

@@ -28,7 +28,9 @@ enum gc_status {
   GC_ENOTPD = 5,      /* Cholesky found A+B not positive definite */
   GC_ETIMEOUT = 6,    /* a bounded device wait ran out */
   GC_ENOMEM = 7,      /* device allocation failed */
-  GC_EUNSUPPORTED = 8 /* shape or mode the library does not handle */
+  GC_EUNSUPPORTED = 8, /* shape or mode the library does not handle */
+  GC_ENONFINITE = 9   /* a NaN or infinity in the inputs (occupations, one-electron
+                         integrals, 2-RDM), in A+-B before the eigensolve, or in W */
 };
 
 /* Arithmetic of the integral transform and of the integrand contraction. */
@@ -77,6 +79,14 @@ int gc_set_eig_refinement(gc_context *ctx, int iterations);
  * products is blocked (order 256 diagonal blocks by dpotrf, panels by dtrsm,
  * trailing updates on the sliced GEMM) for N >= 1536; on = 0: one FP64 dpotrf. */
 int gc_set_chol_blocked(gc_context *ctx, int on);
+/* Limit, in nanoseconds, of every pipeline wait of the tensor-core GEMM kernels
+ * launched on the context (default and maximum 1 s; 0 restores the default).
+ * A wait that runs out makes the kernel stop issuing work, wait (1 s at most)
+ * for the copies and products it already issued, free its tensor memory and
+ * raise a device flag; the call then returns GC_ETIMEOUT and the context stays
+ * usable. Shortening the limit is a fault-injection setting for tests; no
+ * counterpart in the reference. */
+int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns);
 /* Counters of GC_ERPA_CHOLESKY_REFINED on a context: solves, solves that fell back to
  * dsyevd, and the largest cluster of close eigenvalues diagonalised in a block. */
 int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,
@@ -156,16 +166,18 @@ int gc_ace_ne_erpa_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndi
                         const double *fofo_dev, int precision, double *w_host);
 
 /* W(lambda) as gc_ace_ne_erpa_fofo computes it, for callers that cannot
- * allocate device memory (a host whose device memory belongs to its own pool,
- * code running during CUDA graph capture, a process that must not grow its
- * device footprint). It allocates nothing: its working data lives in one fixed
- * device array of this library (about 200 KB, held by every device that loads
- * the library until the process exits), which limits it to nbas <= 2048 and
- * ndimx <= 16384; larger sizes return GC_EINVAL. The first call on a device
- * looks up that array's device address, so make it before any stream capture.
- * Every call shares the array: calls that overlap on the GPU (other streams,
- * other contexts on the device) race. FP64 throughout; no counterpart routine
- * in the reference. */
+ * allocate device memory: a host whose device memory belongs to its own pool,
+ * or a process that must not grow its device footprint after start-up. It
+ * allocates nothing: its working data lives in one fixed device array of this
+ * library (155 904 bytes, held by every device that loads the library until
+ * the process exits), which limits it to nbas <= 2048 and ndimx <= 16384;
+ * larger sizes return GC_EINVAL. The call must be made with the context's
+ * device current (GC_EINVAL otherwise). The first call on a device looks up
+ * that array's device address, so make it before any stream capture. Every
+ * call shares the array: calls that overlap on the GPU (other streams, other
+ * contexts on the device) race. The call waits for its result on the
+ * context's stream. FP64 throughout, about ndimx^3 multiply-adds; no
+ * counterpart routine in the reference. */
 int gc_ace_ne_erpa_fofo_noalloc(gc_context *ctx, int nbas, int ninact, int nact,
                                 int ndimx, const double *occ_host,
                                 const int *indn_host, const double *eigvec_dev,
@@ -224,7 +236,8 @@ typedef struct gc_ac_params {
  * runs one system per process). ecorr/ecas (nsys), w_lambda (nsys*ngrid, may be
  * NULL), omega_stats (nsys*ngrid*GC_OMEGA_STATS, may be NULL). status (nsys, may
  * be NULL): per-system gc_status; when given, systems with A+B not positive
- * definite (GC_ENOTPD) are reported there instead of failing the call. */
+ * definite (GC_ENOTPD) or with non-finite inputs (GC_ENONFINITE) are reported
+ * there instead of failing the call. */
 int gc_ac_energy_batched(gc_context *ctx, int nsys, const gc_system *sys,
                          const gc_ac_params *par, double *ecorr, double *ecas,
                          double *w_lambda, double *omega_stats, int *status);
@@ -282,8 +295,10 @@ int gc_tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k,
                   double *C_dev, int ldc);
 
 /* Average device time of one launch of the tensor-core GEMM kernel for an
- * m x n x k product (operands prepared once, reps launches timed with CUDA
- * events on the context stream). No counterpart in the reference. */
+ * m x n x k product: operands filled with deterministic pseudo-random values
+ * that mix magnitudes over six decades in every row, prepared once, then one
+ * untimed launch and reps launches timed with CUDA events on the context
+ * stream. No counterpart in the reference. */
 int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int k, int reps,
                     double *ms_per_launch);
 

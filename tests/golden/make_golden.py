@@ -29,11 +29,17 @@ def main(seed: int = 0):
                                       ngrid=5)
     print(f"seed {seed}: N={len(indn)} E_CAS={ecas:.12f} (CI {s.e_cas:.12f}) "
           f"ECorr={ecorr:.12f} W={ws} [{time.time() - t0:.0f}s]")
+    # the 8-point rule of the batched configurations, for the measured form's tests
+    _, ecorr8, ws8, x8, w8 = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo,
+                                       s.rdm2act, ngrid=8)
+    print(f"8 points: ECorr={ecorr8:.12f}")
     np.savez_compressed(
         Path(__file__).parent / "ac_cas_n64.npz", n=s.n, nin=s.nin, nact=s.nact, rank=s.rank,
-        seed=seed, lfac=s.lfac, cmo=s.cmo, occ=s.occ, xone=s.xone, rdm2act=s.rdm2act,
-        indn=indn, ngrid=5, x=x, w=w, ecas=ecas, ecorr=ecorr, w_lambda=np.array(ws),
-        e_ci=s.e_cas, ffoo_sum=ffoo.sum(), fofo_sum=fofo.sum())
+        seed=seed, nele=s.nele, lfac=s.lfac, cmo=s.cmo, occ=s.occ, xone=s.xone,
+        rdm2act=s.rdm2act, indn=indn, ngrid=5, x=x, w=w, ecas=ecas, ecorr=ecorr,
+        w_lambda=np.array(ws), x8=x8, w8=w8, ecorr8=ecorr8, w_lambda8=np.array(ws8),
+        e_ci=s.e_cas, fock_diag=np.asarray(s.extra.get("fock_diag", np.zeros(s.n))),
+        ffoo_sum=ffoo.sum(), fofo_sum=fofo.sum())
 
 
 if __name__ == "__main__":

@@ -1,9 +1,10 @@
 """The allocation-free integrand entry point against the regular one.
 
 Some callers of this library cannot allocate device memory when they need
-W(lambda) (their device memory belongs to their own pool, or they are inside
-a CUDA graph capture). gc_ace_ne_erpa_fofo_noalloc serves them from one fixed
-device array; this test calls it twice in a row through the C ABI and checks
+W(lambda): their device memory belongs to their own pool, or their device
+footprint must not grow after start-up. gc_ace_ne_erpa_fofo_noalloc serves
+them from one fixed device array; this test calls it twice in a row through
+the C ABI and checks
 both results against gc_ace_ne_erpa_fofo within the 1e-9 Eh tolerance of the
 other integrand tests. The file sorts last so that a run stopping at the first
 failure has run every other test before it.
@@ -60,3 +61,20 @@ def test_noalloc_rejects_sizes_beyond_its_array(gpu_lib):
                                          dummy, dummy, dummy, C.byref(w))
     assert rc == 1  # GC_EINVAL
     assert "limits" in lib.gc_last_error(ctx.h).decode()
+
+
+def test_noalloc_wrapper_rejects_wrong_layouts(gpu_lib):
+    s = small_system(n=16, nin=2, nact=4, rank=60, seed=0)
+    G, ffoo, fofo = oracle_integrals(s)
+    indn = R.pair_space(s.occ, s.nele)
+    N = len(indn)
+    dev = "cuda:0"
+    y = torch.zeros((N, N), dtype=torch.float64, device=dev).t()
+    e = torch.ones(N, dtype=torch.float64, device=dev)
+    f = torch.as_tensor(fofo, device=dev)
+    with pytest.raises(ValueError):
+        api.ace_ne_erpa_fofo_noalloc(y, e.float(), s.occ, indn, s.nact, s.nin, f)
+    with pytest.raises(ValueError):
+        api.ace_ne_erpa_fofo_noalloc(y, e[::1].repeat(2)[::2], s.occ, indn, s.nact, s.nin, f)
+    with pytest.raises(ValueError):
+        api.ace_ne_erpa_fofo_noalloc(y, e, s.occ, indn, s.nact, s.nin, f.t())
