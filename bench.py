@@ -14,14 +14,20 @@ an affine A+-B with the eigensolve in FP32 refined to FP64 accuracy, concurrent
 worker streams, and the integrand surrogate (ERPA at the two end nodes of the
 8-point rule, an ensemble estimate, and the six interior nodes where the
 estimate exceeds 1 microhartree, on integrals and A+-B kept on the device by a
-batch session between the two passes); the plain FP64
-GPU path (ERPASYMM1, A+-B reassembled per point, one stream) is timed on every
-8th system together with the fast form on the same systems, and every fast
-energy of that subset is checked against the plain FP64 energy (1 microhartree).
+batch session between the two passes). After the timed steps the plain FP64
+GPU path (ERPASYMM1 with FP64 products, A+-B reassembled per point) runs on the
+whole batch with the same worker streams, timed with CUDA events, and every
+energy of the last timed step is checked against it (1 microhartree).
 
---impl reference times the CPU restatement of the reference algorithm (the
-reference itself cannot be compiled here: no Fortran compiler) on a bounded
-sample: the smallest system of the batch, 8 lambda points.
+--impl reference times the reference's algorithm on the host cores (the
+reference itself cannot be compiled here: no Fortran compiler, no MKL): the
+multi-threaded CPU port oracle/cpu_port.py (A+-B reassembled at every point,
+ERPASYMM1 with two LAPACK dsyevd, the integrand as one GEMM) on a fixed
+stratified sample of the same batch -- every 8th system in order of ERPA
+dimension up to the 41st, one system per step. The sample's energies/s
+overstate the CPU's rate on the whole batch (its cost grows as N^3), so the
+ratio against it is a lower bound; an N^3 fit of the sample's times gives the
+whole-batch estimate that is reported beside it.
 """
 from __future__ import annotations
 
@@ -52,7 +58,6 @@ def parse():
     ap.add_argument("--nstreams", type=int, default=8,
                     help="worker streams of the batch; 0 chooses them with api.autotune_streams")
     ap.add_argument("--precision", default="fp64tc5")
-    ap.add_argument("--subset-stride", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--eig-emulation", type=int, default=0)
     ap.add_argument("--erpa", default="refined", choices=["cholesky", "refined"],
@@ -63,7 +68,8 @@ def parse():
     ap.add_argument("--threshold", type=float, default=1e-6)
     ap.add_argument("--gen", default="device", choices=["device", "cpu"],
                     help="input generator: FP64 torch on the GPU, or numpy on the host")
-    ap.add_argument("--no-subset", action="store_true")
+    ap.add_argument("--no-subset", action="store_true",
+                    help="skip the plain FP64 GPU path on the whole batch (comparison and check)")
     ap.add_argument("--kernel-only", type=int, default=0,
                     help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -109,6 +115,12 @@ def max_over_ranks(values, world: int, device):
 def whole_job_rate(world: int, nsys: int, ms: float) -> float:
     """Energies per second of the whole job: every rank's systems over the slowest rank."""
     return world * nsys / (ms / 1000.0)
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the sliced
+# GEMM at the bench's roofline shape, from a one-launch ncu capture of
+# `bench.py --kernel-only N --precision P` (summarised under profiles/).
+GEMM_TRAFFIC: dict = {}
 
 
 def read_peaks():
@@ -196,47 +208,118 @@ def make_batch(nsys, seed, device, run, rank_offset=0, log=print, gen="device"):
     raise RuntimeError("could not find positive-definite systems")
 
 
-def cpu_oracle_sample(batch_systems, ngrid, log=print):
-    """Oracle ACECORR on the smallest system of the batch; energies/s."""
-    import numpy as np
+# positions, in increasing ERPA dimension, of the systems of the batch that the
+# CPU baseline runs (a stratified sample of the lower two thirds of the batch)
+CPU_SAMPLE = (0, 8, 16, 24, 32, 40)
+
+
+def pair_count(sh) -> int:
+    """NDimX of a shape (accas.f:58-99: all pairs minus inactive-inactive and virtual-virtual)."""
+    n, nin, na = sh["n"], sh["nin"], sh["nact"]
+    nv = n - nin - na
+    return n * (n - 1) // 2 - nin * (nin - 1) // 2 - nv * (nv - 1) // 2
+
+
+def workload_config(args) -> dict:
+    """The workload both arms report (the method is reported separately)."""
+    return {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
+            "seed": args.seed, "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"}
+
+
+def cpu_port_energies(systems, ngrid, log=print):
+    """Time the CPU port of the reference algorithm on the given systems; returns
+    (seconds per system, energies, ERPA dimensions)."""
     from oracle import ac_cas_ref as R
-    s = min(batch_systems, key=lambda x: x.n * x.nocc)
-    G = s.ao_eri_packed()
-    t0 = time.time()
-    ffoo, fofo = R.transform_fofo_ffoo(s.cmo, G, s.nin, s.nact)
-    indn = R.pair_space(s.occ, s.nele)
-    ecas, ecorr, ws, x, w = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act,
-                                      ngrid=ngrid)
-    dt = time.time() - t0
-    sample = (f"oracle (numpy/scipy restatement) ACECORR, {ngrid} points, smallest batch system "
-              f"n={s.n} nin={s.nin} CAS({s.nact},{s.nact}) N={len(indn)}, {dt:.1f}s")
-    log(sample)
-    return 1.0 / dt, sample, ecorr
+    from oracle import cpu_port
+    cpu_port.load()
+    times, energies, dims = [], [], []
+    for s in systems:
+        t0 = time.perf_counter()
+        _, ecorr, _ = cpu_port.energy_of_system(s, ngrid=ngrid)
+        times.append(time.perf_counter() - t0)
+        energies.append(ecorr)
+        dims.append(len(R.pair_space(s.occ, s.nele)))
+        log(f"cpu port: N={dims[-1]} {times[-1]:.2f}s")
+    return times, energies, dims
+
+
+def batch_estimate(times, dims, all_dims):
+    """Whole-batch energies/s from a t = c N^3 least-squares fit of the sample."""
+    import numpy as np
+    t, n3 = np.asarray(times), np.asarray(dims, dtype=float) ** 3
+    c = float((t * n3).sum() / (n3 * n3).sum())
+    total = c * float((np.asarray(all_dims, dtype=float) ** 3).sum())
+    return len(all_dims) / total, c
+
+
+def cpu_threads() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
 
 
 def run_reference(args):
+    """The reference's algorithm on the host cores, on a stratified sample of the batch."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
+    import numpy as np
     from gammcor_gb300 import synth
+    from oracle import ac_cas_ref as R
+    from oracle import cpu_port
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
     shapes = synth.batched_shapes(count=args.nsys, seed=args.seed)
-    sh = min(shapes, key=lambda x: x["n"] * (x["nin"] + x["nact"]))
-    s = synth.make_system(sh["n"], sh["nin"], sh["nact"], sh["rank"], sh["seed"])
-    cores = os.cpu_count()
-    vals = []
-    for _ in range(max(1, args.warmup and 1)):
-        v, sample, _ = cpu_oracle_sample([s], args.ngrid, log=lambda *a: None)
-    for _ in range(args.steps):
-        v, sample, _ = cpu_oracle_sample([s], args.ngrid, log=lambda *a: None)
-        vals.append(v)
-    value = statistics.mean(vals)
+    dims = [pair_count(sh) for sh in shapes]
+    order = np.argsort(dims, kind="stable")
+    picks = [int(order[k]) for k in CPU_SAMPLE if k < len(order)]
+    x, w = R.gauleg(0.0, 1.0, args.ngrid)
+    systems = []
+    for i in picks:
+        sh = shapes[i]
+        # the same inputs as the GPU arm: a seed whose A+B is not positive definite at a
+        # quadrature point is replaced as make_batch replaces it
+        for attempt in range(8):
+            seed = sh["seed"] + 100000 * attempt
+            s = synth.make_system(sh["n"], sh["nin"], sh["nact"], sh["rank"], seed)
+            indn = R.pair_space(s.occ, s.nele)
+            ffoo, fofo = cpu_port.transform_factored(s.cmo, s.lfac, s.nin, s.nact)
+            ok = True
+            for lam in x:
+                abp, _, _ = cpu_port.ab_cas_fofo(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo,
+                                                 s.rdm2act, lam)
+                try:
+                    np.linalg.cholesky(0.5 * (abp + abp.T))
+                except np.linalg.LinAlgError:
+                    ok = False
+                    break
+            if ok:
+                break
+        systems.append(s)
+    log(f"reference sample: systems {picks}, N {[len(R.pair_space(s.occ, s.nele)) for s in systems]}")
+    for k in range(args.warmup):
+        cpu_port_energies([systems[k % len(systems)]], args.ngrid, log=lambda *a: None)
+    times, sdims = [], []
+    for k in range(args.steps):
+        t, _, d = cpu_port_energies([systems[k % len(systems)]], args.ngrid, log=log)
+        times += t
+        sdims += d
+    value = len(times) / sum(times)
+    est, c = batch_estimate(times, sdims, dims)
+    threads = cpu_threads()
+    sample = (f"CPU port of the reference algorithm (oracle/cpu_port.py: A+-B reassembled per "
+              f"point with OpenMP, ERPASYMM1 with two LAPACK dsyevd, BLAS products), "
+              f"{args.ngrid} points, one system per step cycling over the systems at positions "
+              f"{list(CPU_SAMPLE)} of the batch ordered by ERPA dimension (N {sorted(set(sdims))}); "
+              f"energies/s of the sample")
     line = {"metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample": "smallest system of the batch"},
-            "cpu_baseline": {"value": value, "unit": "energies/s", "cores": cores, "kind": "port",
-                             "sample": sample},
+            "data": "synthetic", "impl": "reference", "config": workload_config(args),
+            "method": "reference algorithm on the host cores (CPU port; the Fortran reference "
+                      "cannot be compiled here)",
+            "cpu_baseline": {"value": value, "unit": "energies/s", "cores": threads, "kind": "port",
+                             "sample": sample,
+                             "batch_estimate": {"value": est, "unit": "energies/s",
+                                                "model": f"t = {c:.3e} s * N^3 fitted to the "
+                                                         "sample, summed over the 64 systems"}},
             "e2e": {"value": value, "unit": "energies/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -337,6 +420,7 @@ def run_ours(args):
     barrier()
     stream = torch.cuda.current_stream()
     l0 = ctx.launches()
+    eig0 = ctx.eig_time()
     ms = ems = 0.0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -354,80 +438,91 @@ def run_ours(args):
     ms /= args.steps
     ems /= args.steps
     launches = (ctx.launches() - l0) // args.steps
+    eig1 = ctx.eig_time()
+    eig = {"device_ms_per_step": (eig1[0] - eig0[0]) / args.steps,
+           "calls_per_step": (eig1[1] - eig0[1]) // args.steps,
+           "what": "cuSOLVER eigensolves (ssyevd of the refined form, dsyevd fallbacks), CUDA "
+                   "events around each call, summed over the concurrent worker streams"}
     ms, ems = max_over_ranks([ms, ems], world, dev)
     value = whole_job_rate(world, args.nsys, ms)
     e2e = {"value": whole_job_rate(world, args.nsys, ems), "unit": "energies/s",
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     log(f"step: {ms:.0f} ms, {value:.3f} energies/s (e2e {e2e['value']:.3f}), fallback "
-        f"{fb.mean():.2f}, {launches} kernels/step")
+        f"{fb.mean():.2f}, {launches} kernels/step, eigensolves {eig['device_ms_per_step']:.0f} "
+        f"ms in {eig['calls_per_step']} calls")
 
-    # plain FP64 GPU path and the measured step on the same subset; error check
-    sub, t_plain, t_fast_sub, err = [], float("nan"), float("nan"), np.zeros(1)
+    # The plain FP64 GPU path (ERPASYMM1 with FP64 products, A+-B reassembled at every
+    # point) on the whole batch with the same worker streams, timed with CUDA events; every
+    # energy of the last timed step is checked against it.
+    plain = None
     if not args.no_subset:
-        sub = list(range(0, args.nsys, args.subset_stride))
-        sb = batch.subset(sub)
-        plain = dict(ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
-                     nstreams=1)
-        api.ac_energy_batched(sb, **plain)  # warm-up of the plain configuration
+        pl = dict(ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
+                  nstreams=args.nstreams)
         torch.cuda.synchronize()
-        t0 = time.time()
-        pe = api.ac_energy_batched(sb, **plain)[0]
-        torch.cuda.synchronize()
-        t_plain = time.time() - t0
-        t0 = time.time()
-        fe = step(sb)[0]
-        torch.cuda.synchronize()
-        t_fast_sub = time.time() - t0
-        err = np.abs(fe - pe)
-        log(f"subset {sub}: plain FP64 {t_plain:.1f}s, measured step {t_fast_sub:.1f}s, "
-            f"max |dE| {err.max():.2e}")
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as pclk:
+            p0.record(stream)
+            pe, _, _, pst = api.ac_energy_batched(batch, **pl)
+            p1.record(stream)
+            torch.cuda.synchronize()
+        t_plain = p0.elapsed_time(p1)
+        good = (pst == 0) & (status == 0)
+        err = np.abs(ecorr - pe)[good]
+        plain = {"systems": int(good.sum()), "plain_ms": t_plain, "step_ms": ms,
+                 "speedup": t_plain / ms, "streams": args.nstreams,
+                 "max_abs_err_eh": float(err.max()) if err.size else None,
+                 "within_1ueh": bool(err.size and err.max() <= 1e-6),
+                 "timing": "CUDA events on the calling stream, whole batch",
+                 "clocks": pclk.summary()}
+        log(f"plain FP64 on all {int(good.sum())} systems: {t_plain / 1000:.1f}s vs step "
+            f"{ms / 1000:.1f}s ({t_plain / ms:.2f}x), max |dE| {plain['max_abs_err_eh']:.2e}")
 
-    # roofline of this library's dominant kernel: the tcgen05 GEMM at the
-    # integrand shape of the largest system (N x N x N), timed alone
+    # Roofline of this library's dominant kernel: the sliced tcgen05 GEMM at the integrand
+    # shape of the largest system (N x N x N), on mixed-magnitude operands, timed alone.
+    # Its algorithmic work is 2 N^3 (the FP64-accurate product); the BF16 passes it issues
+    # for that are reported beside it.
     hbm, bf16, src = read_peaks()
     Nmax = max(Ns)
     npass = {"bf16x3": 3, "bf16x6": 6, "fp64tc5": 15, "fp64tc6": 21}[args.precision]
     ms_k = api.tc_gemm_time(Nmax, Nmax, Nmax, args.precision, reps=5)
-    ach = 2.0 * Nmax ** 3 * npass / (ms_k / 1000.0) / 1e12
-    # DRAM bytes (read + write) of one 4096^3 FP64TC5 launch from an ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum = 2.5430 GB + 0.1375 GB), scaled
-    # to this launch by the units processed (operand tiles re-read per output tile:
-    # proportional to M N K at equal L2 hit rate).
-    traffic = 2.6806e9 * (Nmax / 4096.0) ** 3 if args.precision == "fp64tc5" else None
+    ach = 2.0 * Nmax ** 3 / (ms_k / 1000.0) / 1e12
     roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-            "frac": ach / bf16, "traffic": traffic, "traffic_unit": "bytes",
-            "traffic_source": "ncu, 4096^3 launch scaled by (N/4096)^3", "peak_source": src,
-            "kernel": f"tcgen05 GEMM ({args.precision}) {Nmax}^3 x {npass} BF16 passes, "
-                      f"{ms_k:.2f} ms/launch"}
+            "frac": ach / bf16, "traffic": GEMM_TRAFFIC.get((args.precision, Nmax)),
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + write.sum)",
+            "peak_source": src,
+            "passes": {"count": npass, "achieved": ach * npass, "frac": ach * npass / bf16},
+            "kernel": f"k_tc_gemm_oz ({args.precision}) {Nmax}^3, {ms_k:.2f} ms/launch"}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        v, sample, _ = cpu_oracle_sample(batch.systems, args.ngrid, log=log)
-        cpu = {"value": v, "unit": "energies/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": sample}
+        order = np.argsort(Ns, kind="stable")
+        picks = [int(order[k]) for k in CPU_SAMPLE[:4] if k < len(order)]
+        times, _, dims = cpu_port_energies([batch.systems[i] for i in picks], args.ngrid, log=log)
+        est, _ = batch_estimate(times, dims, Ns)
+        cpu = {"value": len(times) / sum(times), "unit": "energies/s", "cores": cpu_threads(),
+               "kind": "port",
+               "sample": f"CPU port of the reference algorithm (oracle/cpu_port.py), "
+                         f"{args.ngrid} points, systems {picks} of this batch (N {dims}), "
+                         f"{sum(times):.1f}s; energies/s of the sample",
+               "batch_estimate": {"value": est, "unit": "energies/s",
+                                  "model": "t = c N^3 fitted to the sample"}}
 
     if rank == 0:
+        method = {"precision": args.precision,
+                  "erpa": ("cholesky(A+B), affine A+-B, " +
+                           ("FP32 eigensolve refined to FP64 accuracy "
+                            f"({args.eig_refine} iteration(s))"
+                            if args.erpa == "refined" else "FP64 dsyevd")),
+                  "streams": args.nstreams, "streams_autotune": tuned,
+                  "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens else "off"),
+                  "eig_emulation": bool(args.eig_emulation)}
         line = {"metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic",
-                "config": {"workload": WORKLOAD, "nsys": args.nsys, "lambda_points": args.ngrid,
-                           "precision": args.precision, "erpa": ("cholesky(A+B), affine A+-B, " +
-                                    ("FP32 eigensolve refined to FP64 accuracy "
-                                     f"({args.eig_refine} iteration(s))"
-                                     if args.erpa == "refined" else "FP64 dsyevd")),
-                           "streams": args.nstreams, "streams_autotune": tuned,
-                           "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens
-                                         else "off"),
-                           "eig_emulation": bool(args.eig_emulation),
-                           "l2": "inputs larger than L2 (per-system factor + FFOO/FOFO)"},
+                "data": "synthetic", "config": workload_config(args), "method": method,
                 "surrogate_fallback_rate": float(fb.mean()),
-                "plain_fp64_subset": {"systems": sub,
-                                      "plain_s": t_plain if sub else None,
-                                      "step_s": t_fast_sub if sub else None,
-                                      "speedup": t_plain / t_fast_sub if sub else None,
-                                      "max_abs_err_eh": float(err.max()),
-                                      "within_1ueh": bool(err.max() <= 1e-6)},
+                "erpa_solves_per_energy": float(2 + 6 * fb.mean()) if ens else float(args.ngrid),
+                "plain_fp64": plain, "eigensolve": eig,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk.summary(), "failed_systems": int((status != 0).sum()),
                 "eig_refine_stats": ctx.eig_refine_stats()}

@@ -49,6 +49,12 @@ class Context:
     def launches(self) -> int:
         return int(load().gc_kernel_launches(self.h))
 
+    def eig_time(self) -> tuple[float, int]:
+        """(milliseconds, calls) of the cuSOLVER eigensolves run on this context so far."""
+        ms, n = C.c_double(), C.c_longlong()
+        check(self.h, load().gc_eig_time(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
     def sync(self):
         check(self.h, load().gc_synchronize(self.h))
 

@@ -56,7 +56,9 @@ int gc_create(gc_context **out, int device, void *stream) {
   if (cudaMalloc(&ctx->dev_info, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&ctx->dev_flag, sizeof(int)) != cudaSuccess ||
       cudaMemset(ctx->dev_flag, 0, sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&ctx->dev_nonfinite, sizeof(int)) != cudaSuccess) {
+      cudaMalloc(&ctx->dev_nonfinite, sizeof(int)) != cudaSuccess ||
+      cudaEventCreate(&ctx->eig_ev[0]) != cudaSuccess ||
+      cudaEventCreate(&ctx->eig_ev[1]) != cudaSuccess) {
     gc_destroy(ctx);
     return GC_ENOMEM;
   }
@@ -72,6 +74,8 @@ int gc_destroy(gc_context *ctx) {
   if (ctx->dev_info) cudaFree(ctx->dev_info);
   if (ctx->dev_flag) cudaFree(ctx->dev_flag);
   if (ctx->dev_nonfinite) cudaFree(ctx->dev_nonfinite);
+  for (cudaEvent_t e : ctx->eig_ev)
+    if (e) cudaEventDestroy(e);
   delete ctx;
   return GC_OK;
 }
@@ -85,6 +89,13 @@ int gc_synchronize(gc_context *ctx) {
 }
 
 long long gc_kernel_launches(const gc_context *ctx) { return ctx ? ctx->launches : 0; }
+
+int gc_eig_time(const gc_context *ctx, double *ms, long long *calls) {
+  if (!ctx) return GC_EINVAL;
+  if (ms) *ms = ctx->eig_ms;
+  if (calls) *calls = ctx->eig_calls;
+  return GC_OK;
+}
 
 int gc_set_eig_emulation(gc_context *ctx, int on) {
   if (!ctx) return GC_EINVAL;

@@ -202,7 +202,10 @@ int run_tasks(gc_context *ctx, std::vector<Worker> &ws, int ntask,
     ctx->refine_solves += w.ctx->refine_solves;
     ctx->refine_fallbacks += w.ctx->refine_fallbacks;
     ctx->refine_max_cluster = std::max(ctx->refine_max_cluster, w.ctx->refine_max_cluster);
-    w.ctx->launches = w.ctx->refine_solves = w.ctx->refine_fallbacks = 0;
+    ctx->eig_ms += w.ctx->eig_ms;
+    ctx->eig_calls += w.ctx->eig_calls;
+    w.ctx->launches = w.ctx->refine_solves = w.ctx->refine_fallbacks = w.ctx->eig_calls = 0;
+    w.ctx->eig_ms = 0.0;
   }
   cudaEventDestroy(start);
   if (first_err.load() != GC_OK)

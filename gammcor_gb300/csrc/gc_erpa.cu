@@ -108,18 +108,31 @@ __global__ void k_sqrt_eig(int N, double *__restrict__ eig) {
   if (i < N && eig[i] > kSmall) eig[i] = sqrt(eig[i]);
 }
 
+// Adds the device time between the context's two eigensolve events (recorded around
+// the cuSOLVER call, already complete: the caller synchronised).
+int add_eig_time(gc_context *ctx) {
+  float ms = 0.f;
+  GC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->eig_ev[0], ctx->eig_ev[1]));
+  ctx->eig_ms += ms;
+  ctx->eig_calls++;
+  return GC_OK;
+}
+
 int syevd(gc_context *ctx, int N, double *A, double *w) {
   int lwork = 0;
   GC_CUSOLVER(ctx, cusolverDnDsyevd_bufferSize(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR,
                                                CUBLAS_FILL_MODE_LOWER, N, A, N, w, &lwork));
   gc::DevBuf<double> work;
   GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
+  GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[0], ctx->stream));
   GC_CUSOLVER(ctx, cusolverDnDsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
                                     N, A, N, w, work.p, lwork, ctx->dev_info));
+  GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[1], ctx->stream));
   int info = 0;
   GC_CUDA(ctx, cudaMemcpyAsync(&info, ctx->dev_info, sizeof(int), cudaMemcpyDeviceToHost,
                                ctx->stream));
   GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  GC_TRY(add_eig_time(ctx));
   if (info != 0) return gc::set_error(ctx, GC_ECUSOLVER, "dsyevd info=%d (N=%d)", info, N);
   return GC_OK;
 }
@@ -571,9 +584,11 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
     GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
     if (ctx->eig_emulation)
       GC_CUSOLVER(ctx, cusolverDnSetMathMode(ctx->cusolver, CUSOLVER_FP32_EMULATED_BF16X9_MATH));
+    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[0], ctx->stream));
     cusolverStatus_t st = cusolverDnSsyevd(ctx->cusolver, CUSOLVER_EIG_MODE_VECTOR,
                                            CUBLAS_FILL_MODE_LOWER, N, m32.p, N, w32.p, work.p, lwork,
                                            ctx->dev_info);
+    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[1], ctx->stream));
     if (ctx->eig_emulation)
       GC_CUSOLVER(ctx, cusolverDnSetMathMode(ctx->cusolver, CUSOLVER_DEFAULT_MATH));
     GC_CUSOLVER(ctx, st);
@@ -582,6 +597,7 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
     GC_CUDA(ctx, cudaMemcpyAsync(&info, ctx->dev_info, sizeof(int), cudaMemcpyDeviceToHost,
                                  ctx->stream));
     GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    GC_TRY(add_eig_time(ctx));
     if (info != 0) {
       *fallback = true;
       return GC_OK;

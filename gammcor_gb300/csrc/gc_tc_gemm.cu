@@ -71,26 +71,29 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(addr), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded parity wait: returns false if the phase did not complete within limit_ns.
+// try_wait itself suspends the thread for a while, so the timer is read once per
+// unsuccessful attempt (never when the first attempt succeeds).
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
                                           unsigned long long limit_ns) {
-  uint32_t addr = smem_u32(bar);
-  unsigned long long t0 = 0;
-  for (unsigned it = 0;; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(addr), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if ((it & 255) == 0) {
-      unsigned long long t = globaltimer();
-      if (t0 == 0) t0 = t;
-      else if (t - t0 > limit_ns) return false;
-    }
+  const uint32_t addr = smem_u32(bar);
+  if (mbar_try(addr, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (;;) {
+    if (mbar_try(addr, parity)) return true;
+    if (globaltimer() - t0 > limit_ns) return false;
   }
 }
 

@@ -67,6 +67,11 @@ const char *gc_last_error(const gc_context *ctx);
 int gc_synchronize(gc_context *ctx);
 /* Number of kernels of this library launched on the context so far. */
 long long gc_kernel_launches(const gc_context *ctx);
+/* Device time (CUDA events) of the cuSOLVER eigensolves run on the context so far
+ * (dsyevd of ERPASYMM1 and of the Cholesky form, ssyevd of the refined form), and
+ * their number; batched calls add their workers' eigensolves. No counterpart in
+ * the reference. */
+int gc_eig_time(const gc_context *ctx, double *ms, long long *calls);
 /* on = 1 lets cuSOLVER run the FP64 eigensolver's internal matrix products with
  * its fixed-point FP64 emulation on tensor cores (cusolverDnSetEmulationStrategy
  * EAGER), and the FP32 eigensolver of GC_ERPA_CHOLESKY_REFINED with BF16x9
