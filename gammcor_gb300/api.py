@@ -185,9 +185,11 @@ def tran4_factored(nbas: int, lfac: torch.Tensor, CA, CB, CC, CD, precision: str
 # ------------------------------------------------------------------ assembly
 def ab_cas_fofo(occ: np.ndarray, xone: np.ndarray, indn: np.ndarray, nact: int, inactive: int,
                 ffoo: torch.Tensor, fofo: torch.Tensor, rdm2act: np.ndarray, acalpha: float,
-                ctx: Context | None = None):
+                ure: np.ndarray | None = None, ab1: bool = False, ctx: Context | None = None):
     """AB_CAS_FOFO (abfofo.f90:8-293). Returns (ABPLUS, ABMIN, ETot); the
-    matrices are (NDimX, NDimX) views with Fortran meaning (column-major storage)."""
+    matrices are (NDimX, NDimX) views with Fortran meaning (column-major storage).
+    ure: the URe rotation of the one-electron integrals (None: identity); ab1: the
+    AB1 form (the lambda derivative of A+-B)."""
     ctx = ctx or default_context(ffoo.device.index or 0)
     occ = np.ascontiguousarray(occ, dtype=np.float64)
     xone = np.ascontiguousarray(xone, dtype=np.float64)
@@ -195,12 +197,15 @@ def ab_cas_fofo(occ: np.ndarray, xone: np.ndarray, indn: np.ndarray, nact: int, 
     rdm = np.ascontiguousarray(rdm2act, dtype=np.float64)
     n = occ.shape[0]
     N = ind.shape[0] // 2
+    u = None if ure is None else np.asfortranarray(ure, dtype=np.float64)
     abp = torch.empty((N, N), dtype=torch.float64, device=ffoo.device)
     abm = torch.empty_like(abp)
     etot = C.c_double()
-    check(ctx.h, load().gc_ab_cas_fofo(ctx.h, n, inactive, nact, N, _dptr(occ), _dptr(xone),
-                                       _iptr(ind), _dptr(rdm), _ptr(ffoo), _ptr(fofo),
-                                       float(acalpha), _ptr(abp), _ptr(abm), C.byref(etot)))
+    check(ctx.h, load().gc_ab_cas_fofo_ex(ctx.h, n, inactive, nact, N, _dptr(occ),
+                                          _dptr(u.ravel(order="F")) if u is not None else None,
+                                          _dptr(xone), _iptr(ind), _dptr(rdm), _ptr(ffoo),
+                                          _ptr(fofo), float(acalpha), int(ab1), _ptr(abp),
+                                          _ptr(abm), C.byref(etot)))
     return abp.t(), abm.t(), etot.value
 
 
@@ -221,6 +226,19 @@ def erpasymm1(abplus: torch.Tensor, abmin: torch.Tensor, mode: str = "symm1",
     check(ctx.h, load().gc_erpa_ex(ctx.h, N, _ptr(ap), _ptr(am), _ptr(y), _ptr(eig), ERPA[mode],
                                    PREC[precision]))
     return y.t(), eig
+
+
+def erpasymm1_aplsqrt(abplus: torch.Tensor, abmin: torch.Tensor, ctx: Context | None = None):
+    """ERPASYMM1 (interpa.f:1652-1781) with the routine's APLSQRT output: returns
+    (EigVecR, Eig, APLSQRT = A+^1/2), all with Fortran meaning. FP64."""
+    ctx = ctx or default_context(abplus.device.index or 0)
+    ap = abplus.t().contiguous()
+    am = abmin.t().contiguous()
+    N = ap.shape[0]
+    y = torch.empty_like(ap)
+    eig = torch.empty(N, dtype=torch.float64, device=ap.device)
+    check(ctx.h, load().gc_erpasymm1(ctx.h, N, _ptr(ap), _ptr(am), _ptr(y), _ptr(eig)))
+    return y.t(), eig, ap.t()
 
 
 def ace_ne_erpa_fofo(evec: torch.Tensor, evals: torch.Tensor, occ: np.ndarray, indn: np.ndarray,

@@ -18,6 +18,12 @@ namespace {
 
 struct Geo {
   int n, nin, nact, nocc;
+  // AB1 = .false.: AuxCoeff = 1 for four equal groups, HNO kept inside a group with the
+  // (1 - lambda) inactive/active correction. AB1 = .true. (the lambda derivative,
+  // abfofo.f90:109-156 and HNOCoef, abfofo.f90:167-171, 4494-4500): AuxCoeff = 0 there,
+  // HNO zeroed inside a group and the correction taken with coefficient -1.
+  double same = 1.0;   // AuxCoeff of four equal groups
+  int ab1 = 0;
 };
 
 __device__ __forceinline__ double Fofo(const double *__restrict__ f, const Geo &g, int a, int b,
@@ -34,9 +40,9 @@ __device__ __forceinline__ double RV(const double *__restrict__ rv, int nocc, in
                                      int l) {
   return rv[i + (size_t)nocc * (j + (size_t)nocc * (k + (size_t)nocc * l))];
 }
-// AuxCoeff(g1,g2,g3,g4): 1 if the four orbital groups are equal, else lambda.
-__device__ __forceinline__ double AC(int a, int b, int c, int d, double lam) {
-  return (a == b && b == c && c == d) ? 1.0 : lam;
+// AuxCoeff(g1,g2,g3,g4): g.same if the four orbital groups are equal, else lambda.
+__device__ __forceinline__ double AC(const Geo &g, int a, int b, int c, int d, double lam) {
+  return (a == b && b == c && c == d) ? g.same : lam;
 }
 // AuxInd(g1,g2) of AB_CAS_FOFO: 1 for inactive/active combinations other than
 // active-active, 2 for active-active, 0 otherwise.
@@ -63,17 +69,17 @@ __global__ void k_onebody(Geo g, const double *__restrict__ h, const double *__r
     double jv = Ffoo(ffoo, g, i, j, k, k);          // (ij|kk)
     double kv = Fofo(fofo, g, j, k, i, k);          // (jk|ik)
     if (gi == gj && gk != gi) corr += ok * (2.0 * jv - kv);
-    double t = ok * (2.0 * AC(gi, gj, gk, gk, lam) * jv - AC(gi, gi, gj, gk, lam) * kv);
+    double t = ok * (2.0 * AC(g, gi, gj, gk, gk, lam) * jv - AC(g, gi, gi, gj, gk, lam) * kv);
     ai += t;
     if (k < g.nin) aio += t;
   }
   size_t o = i + (size_t)j * g.n;
-  hno[o] = (gi != gj) ? lam * hv : hv + (1.0 - lam) * corr;
+  hno[o] = (gi != gj) ? lam * hv : (g.ab1 ? -corr : hv + (1.0 - lam) * corr);
   auxi[o] = ai;
   auxio[o] = aio;
 }
 
-// WMAT(k, r) = sum_{l,i,j < nocc} AC(k,l,i,j) (kl|ij) RDM2val(i,j,r,l); zero for r >= nocc.
+// WMAT(k, r) = sum_{l,i,j < nocc} AuxCoeff(k,l,i,j) (kl|ij) RDM2val(i,j,r,l); zero for r >= nocc.
 __global__ void k_wmat(Geo g, const int *__restrict__ grp, const double *__restrict__ fofo,
                        const double *__restrict__ rv, double lam, double *__restrict__ wmat) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -87,7 +93,7 @@ __global__ void k_wmat(Geo g, const int *__restrict__ grp, const double *__restr
       for (int j = 0; j < g.nocc; ++j) {
         int gj = grp[j];
         for (int i = 0; i < g.nocc; ++i)
-          s += AC(gk, gl, grp[i], gj, lam) * Fofo(fofo, g, k, l, i, j) * RV(rv, g.nocc, i, j, r, l);
+          s += AC(g, gk, gl, grp[i], gj, lam) * Fofo(fofo, g, k, l, i, j) * RV(rv, g.nocc, i, j, r, l);
       }
     }
   }
@@ -300,7 +306,7 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   int gp = grp[p], gq = grp[q], gr = grp[r], gs = grp[s];
   double op = occ[p], oq = occ[q], orr = occ[r], os = occ[s];
   double vp = 0.0, vm = 0.0, v;
-  double ac = AC(gp, gq, gr, gs, lam);
+  double ac = AC(g, gp, gq, gr, gs, lam);
   auto ai = [](int a, int b) { return AuxInd(a, b) == 1; };
   double X1 = (ai(gp, gr) ? op * orr : 0.0) + (ai(gq, gs) ? oq * os : 0.0) -
               (ai(gq, gr) ? oq * orr : 0.0) - (ai(gp, gs) ? op * os : 0.0);
@@ -320,20 +326,20 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   const int pA = p - nin, qA = q - nin, rA = r - nin, sA = s - nin;
   // FOFO T1 (p -> q)
   if (p >= nin && ra && qa) {
-    v = AC(gp, gs, 1, 1, lam) * Z.z1[p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA))];
+    v = AC(g, gp, gs, 1, 1, lam) * Z.z1[p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA))];
     vp += v;
     vm -= v;
   }
   // FOFO T3
   if (r >= nin && sa && pa) {
-    v = AC(gq, gr, 1, 1, lam) * Z.z1[r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA))];
+    v = AC(g, gq, gr, 1, 1, lam) * Z.z1[r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA))];
     vp += v;
     vm -= v;
   }
   if (r >= nin && sa) {
     if (qa && p >= nin) {
       size_t o = r + (size_t)n * (p + (size_t)n * (qA + (size_t)na * sA));
-      double c = AC(gp, gr, 1, 1, lam);
+      double c = AC(g, gp, gr, 1, 1, lam);
       v = c * Z.z4[o];  // T4
       vp += v;
       vm += v;
@@ -343,7 +349,7 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
     }
     if (pa) {
       size_t o = r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA));
-      double c = AC(gq, gr, 1, 1, lam);
+      double c = AC(g, gq, gr, 1, 1, lam);
       v = c * Z.z5[o];  // T4 (p -> q)
       vp += v;
       vm -= v;
@@ -354,7 +360,7 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   }
   if (ra && pa) {
     size_t o = q + (size_t)nocc * (s + (size_t)nocc * (pA + (size_t)na * rA));
-    double c = AC(gq, gs, 1, 1, lam);
+    double c = AC(g, gq, gs, 1, 1, lam);
     v = c * Z.z8[o];  // FFOO T1
     vp += v;
     vm += v;
@@ -366,13 +372,13 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
     vm -= v;
   }
   if (sa && r >= nin && qa && p >= nin) {  // FFOO T3
-    v = AC(gp, gr, 1, 1, lam) * Z.z9[p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA))];
+    v = AC(g, gp, gr, 1, 1, lam) * Z.z9[p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA))];
     vp += v;
     vm += v;
   }
   if (ra && qa && p >= nin) {
     size_t o = p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA));
-    double c = AC(gp, gs, 1, 1, lam);
+    double c = AC(g, gp, gs, 1, 1, lam);
     v = c * Z.z11[o];  // T2 (p -> q)
     vp += v;
     vm -= v;
@@ -412,9 +418,37 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   abm[o] = vm;
 }
 
+// sq_symmetrize (tran.f90:1303-1319): a(i,j) = a(j,i) = (a(i,j) + a(j,i)) / 2.
+__global__ void k_sym_avg(int N, double *__restrict__ a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= N || j >= N || j <= i) return;
+  const size_t u = i + (size_t)j * N, l = j + (size_t)i * N;
+  const double v = 0.5 * (a[u] + a[l]);
+  a[u] = v;
+  a[l] = v;
+}
+
 }  // namespace
 
 namespace gc {
+
+int rotate_h(gc_context *ctx, SysDev &sd, const double *ure_host) {
+  // HNO = URe . h . URe^T, then sq_symmetrize (abfofo.f90:97-100)
+  const int n = sd.n;
+  DevBuf<double> u, w;
+  GC_TRY(u.upload(ctx, ure_host, (size_t)n * n));
+  GC_TRY(w.alloc(ctx, (size_t)n * n));
+  const double one = 1.0, zero = 0.0;
+  GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, u.p, n, sd.h.p, n,
+                             &zero, w.p, n));
+  GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, n, &one, w.p, n, u.p, n,
+                             &zero, sd.h.p, n));
+  dim3 bs(32, 8), gs(ceil_div(n, 32), ceil_div(n, 8));
+  k_sym_avg<<<gs, bs, 0, ctx->stream>>>(n, sd.h.p);
+  GC_LAUNCHED(ctx);
+  return GC_OK;
+}
 
 int set_error(gc_context *ctx, int code, const char *fmt, ...) {
   if (ctx) {
@@ -539,8 +573,8 @@ static int build_z(gc_context *ctx, const SysDev &sd, const double *ffoo, const 
 }
 
 int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
-                double alpha, double *abplus, double *abmin, double *etot_host) {
-  Geo g{sd.n, sd.nin, sd.nact, sd.nocc};
+                double alpha, double *abplus, double *abmin, double *etot_host, int ab1) {
+  Geo g{sd.n, sd.nin, sd.nact, sd.nocc, ab1 ? 0.0 : 1.0, ab1 ? 1 : 0};
   const int n = sd.n, N = sd.ndimx;
   ZBufs Zb;
   GC_TRY(build_z(ctx, sd, ffoo, fofo, Zb));
@@ -562,6 +596,13 @@ int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const dou
   k_ab<<<g3, b3, 0, ctx->stream>>>(g, N, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, ffoo,
                                    Z, hno.p, auxi.p, auxio.p, wmat.p, alpha, abplus, abmin);
   GC_LAUNCHED(ctx);
+  if (ab1) {  // AB_CAS_FOFO symmetrises the AB1 matrices (sq_symmetrize, abfofo.f90:260-263)
+    dim3 bs(32, 8), gs(ceil_div(N, 32), ceil_div(N, 8));
+    k_sym_avg<<<gs, bs, 0, ctx->stream>>>(N, abplus);
+    GC_LAUNCHED(ctx);
+    k_sym_avg<<<gs, bs, 0, ctx->stream>>>(N, abmin);
+    GC_LAUNCHED(ctx);
+  }
   if (etot_host) {
     const int nb = 120;
     DevBuf<double> part;
@@ -586,15 +627,29 @@ int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const dou
 
 }  // namespace gc
 
+extern "C" int gc_ab_cas_fofo_ex(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                                 const double *occ, const double *ure, const double *xone,
+                                 const int *indn, const double *rdm2act, const double *ffoo,
+                                 const double *fofo, double alpha, int ab1, double *abplus,
+                                 double *abmin, double *etot) {
+  if (!ctx) return GC_EINVAL;
+  if (!xone || !ffoo || !fofo || !abplus || !abmin)
+    return gc::set_error(ctx, GC_EINVAL, "ab_cas_fofo: null pointer");
+  if (ure)
+    for (size_t i = 0; i < (size_t)nbas * nbas; ++i)
+      if (!std::isfinite(ure[i]))
+        return gc::set_error(ctx, GC_ENONFINITE, "ab_cas_fofo: non-finite value in URe");
+  gc::SysDev sd;
+  GC_TRY(gc::sys_upload(ctx, sd, nbas, ninact, nact, ndimx, occ, xone, indn, rdm2act));
+  if (ure) GC_TRY(gc::rotate_h(ctx, sd, ure));
+  GC_TRY(gc::assemble_ab(ctx, sd, ffoo, fofo, alpha, abplus, abmin, etot, ab1 ? 1 : 0));
+  return GC_OK;
+}
+
 extern "C" int gc_ab_cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
                               const double *occ, const double *xone, const int *indn,
                               const double *rdm2act, const double *ffoo, const double *fofo,
                               double alpha, double *abplus, double *abmin, double *etot) {
-  if (!ctx) return GC_EINVAL;
-  if (!xone || !ffoo || !fofo || !abplus || !abmin)
-    return gc::set_error(ctx, GC_EINVAL, "ab_cas_fofo: null pointer");
-  gc::SysDev sd;
-  GC_TRY(gc::sys_upload(ctx, sd, nbas, ninact, nact, ndimx, occ, xone, indn, rdm2act));
-  GC_TRY(gc::assemble_ab(ctx, sd, ffoo, fofo, alpha, abplus, abmin, etot));
-  return GC_OK;
+  return gc_ab_cas_fofo_ex(ctx, nbas, ninact, nact, ndimx, occ, nullptr, xone, indn, rdm2act, ffoo,
+                           fofo, alpha, 0, abplus, abmin, etot);
 }

@@ -775,7 +775,7 @@ int eigen(gc_context *ctx, int N, double *M, double *w, int mode, int prec) {
 namespace gc {
 
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig,
-               int mode, int gemm_precision) {
+               int mode, int gemm_precision, bool aplsqrt_out) {
   if (N <= 0 || !abplus || !abmin || !Y || !eig)
     return set_error(ctx, GC_EINVAL, "erpa: bad arguments N=%d", N);
   const size_t NN = (size_t)N * N;
@@ -826,6 +826,9 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
                                &zero, H.p, N));
     k_norm_symm1<<<N, 256, 0, ctx->stream>>>(N, Y, H.p, eig);
     GC_LAUNCHED(ctx);
+    if (aplsqrt_out)  // ERPASYMM1 leaves A+^1/2 in its A+ argument (interpa.f:1652-1716)
+      GC_CUDA(ctx, cudaMemcpyAsync(abplus, P.p, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   ctx->stream));
     return GC_OK;
   }
   if (mode == GC_ERPA_CHOLESKY || mode == GC_ERPA_CHOLESKY_REFINED) {
@@ -893,6 +896,13 @@ extern "C" int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus, double *ab
   if (precision != GC_PREC_FP64 && precision != GC_PREC_FP64TC5 && precision != GC_PREC_FP64TC6)
     return gc::set_error(ctx, GC_EINVAL, "gc_erpa_ex: precision %d is not FP64-accurate", precision);
   GC_TRY(gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, precision));
+  return gc::check_flag(ctx);
+}
+
+extern "C" int gc_erpasymm1(gc_context *ctx, int ndimx, double *abplus, double *abmin,
+                            double *eigvec, double *eig) {
+  if (!ctx) return GC_EINVAL;
+  GC_TRY(gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, GC_ERPA_SYMM1, GC_PREC_FP64, true));
   return gc::check_flag(ctx);
 }
 

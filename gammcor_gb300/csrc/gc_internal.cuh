@@ -133,14 +133,18 @@ int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int 
                const double *occ, const double *xone, const int *indn, const double *rdm2act);
 
 // Assembly (gc_assembly.cu).
+// ab1 = 1: the AB1 form of AB_CAS_FOFO (the lambda derivative, symmetrised).
 int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
-                double alpha, double *abplus, double *abmin, double *etot_host);
+                double alpha, double *abplus, double *abmin, double *etot_host, int ab1 = 0);
+// One-electron matrix of sd rotated in place: h <- URe h URe^T, symmetrised.
+int rotate_h(gc_context *ctx, SysDev &sd, const double *ure_host);
 
 // ERPA (gc_erpa.cu).
 // gemm_precision selects the arithmetic of the similarity and back-transform
 // products of the Cholesky form (GC_PREC_FP64 or a sliced FP64-accurate mode).
+// aplsqrt_out (GC_ERPA_SYMM1 only): A+^1/2 is written over abplus, as ERPASYMM1 does.
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *eigvec,
-               double *eig, int mode, int gemm_precision);
+               double *eig, int mode, int gemm_precision, bool aplsqrt_out = false);
 
 // Integrand (gc_integrand.cu).
 int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,

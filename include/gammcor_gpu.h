@@ -147,7 +147,27 @@ int gc_ab_cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
                    const double *ffoo_dev, const double *fofo_dev, double alpha,
                    double *abplus_dev, double *abmin_dev, double *etot_host);
 
+/* AB_CAS_FOFO with every argument of the reference routine (abfofo.f90:8-10):
+ * ure_host (nbas x nbas, column-major) rotates the one-electron integrals,
+ * HNO = URe h URe^T symmetrised (abfofo.f90:97-100); NULL is the identity, as
+ * LdInteg leaves it. ab1 = 1 returns the AB1 matrices (abfofo.f90:109-171,
+ * 260-263): the lambda derivative of A+-B (AuxCoeff 0 inside one orbital group,
+ * HNO zeroed inside a group, HNOCoef -1), symmetrised; with alpha = 1 it is
+ * A+-B(1) - A+-B(0), as the AC0 and frequency routines use it. */
+int gc_ab_cas_fofo_ex(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                      const double *occ_host, const double *ure_host, const double *xone_host,
+                      const int *indn_host, const double *rdm2act_host,
+                      const double *ffoo_dev, const double *fofo_dev, double alpha, int ab1,
+                      double *abplus_dev, double *abmin_dev, double *etot_host);
+
 /* ERPA ---------------------------------------------------------------------- */
+
+/* ERPASYMM1(EigVecR,Eig,APLSQRT,ABMIN,NBasis,NDimX), interpa.f:1652-1781, with the
+ * reference's argument semantics: abplus_dev holds A+ on entry and A+^1/2 on return
+ * (the routine overwrites APLSQRT), abmin_dev is symmetrised in place, eigvec_dev
+ * receives Y, eig_dev omega (omega^2 where omega^2 <= 1e-6), ascending. FP64. */
+int gc_erpasymm1(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
+                 double *eigvec_dev, double *eig_dev);
 
 /* ERPASYMM1, interpa.f:1652-1781 (mode GC_ERPA_SYMM1), or the Cholesky form.
  * abplus_dev/abmin_dev are read (and symmetrised in place). eigvec_dev(N,N)

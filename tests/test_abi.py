@@ -55,3 +55,14 @@ def test_host_pair_space_matches_oracle(lib):
         assert api.prepare_nums(occ, nele) == R.prepare_nums(occ, nele)
         np.testing.assert_array_equal(api.pair_space(occ, nele, ifl_core=0),
                                       R.pair_space(occ, nele, ifl_core=0))
+
+
+def test_fortran_module_binds_declared_symbols():
+    """Every bind(C) name of the Fortran module is declared in the C header (or is a
+    CUDA runtime call the wrappers use to move their host arrays)."""
+    text = (ROOT / "include" / "gammcor_gpu.f90").read_text()
+    names = set(re.findall(r'bind\(C,\s*name="(\w+)"\)', text))
+    assert {"gc_ab_cas_fofo_ex", "gc_erpasymm1", "gc_ace_ne_erpa_fofo", "gc_tran4_gen"} <= names
+    declared = set(declared_symbols())
+    for nm in names:
+        assert nm in declared or nm in {"cudaMalloc", "cudaFree", "cudaMemcpy"}, nm
