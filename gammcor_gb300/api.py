@@ -288,6 +288,25 @@ def ace_ne_erpa_fofo_noalloc(evec: torch.Tensor, evals: torch.Tensor, occ: np.nd
     return w.value
 
 
+def ac0cas_fofo(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ure=None,
+                ctx: Context | None = None):
+    """AC0CAS_FOFO (abfofo.f90:1485-1750): returns (ECorr, ETot), the AC0 correlation
+    energy and E_CAS (without ENuc)."""
+    ctx = ctx or default_context(ffoo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    xone = np.ascontiguousarray(xone, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    rdm = np.ascontiguousarray(rdm2act, dtype=np.float64)
+    u = None if ure is None else np.asfortranarray(ure, dtype=np.float64)
+    ec, et = C.c_double(), C.c_double()
+    check(ctx.h, load().gc_ac0cas_fofo(ctx.h, occ.shape[0], inactive, nact, ind.shape[0] // 2,
+                                       _dptr(occ),
+                                       _dptr(u.ravel(order="F")) if u is not None else None,
+                                       _dptr(xone), _iptr(ind), _dptr(rdm), _ptr(ffoo), _ptr(fofo),
+                                       C.byref(ec), C.byref(et)))
+    return ec.value, et.value
+
+
 def acecorr(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ngrid: int = 5,
             erpa_mode: str = "symm1", precision: str = "fp64", ctx: Context | None = None):
     """ACECORR (acfd.f:117-209). Returns (E_CAS, ECorr, [W(lambda_i)])."""

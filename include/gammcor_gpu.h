@@ -209,6 +209,22 @@ int gc_ace_ne_erpa_fofo_noalloc(gc_context *ctx, int nbas, int ninact, int nact,
                                 const double *eig_dev, const double *fofo_dev,
                                 double *w_host);
 
+/* AC0 ------------------------------------------------------------------------ */
+
+/* AC0CAS_FOFO, abfofo.f90:1485-1750 (dispatched at acfd.f:64-68): the AC0
+ * correlation energy, first order in the adiabatic connection. A+-B at
+ * lambda = 0 is block diagonal in the pair groups of create_AC0_blocks_1/2
+ * (abfofo.f90:1374-1484); each block's ERPA problem (ERPASYMM0,
+ * interpa.f:1496-1650) is solved on the device in FP64, the AB1 matrices are
+ * taken to the zeroth-order modes and back (abpm_tran, ABPM_BACKTRAN) and
+ * contracted with FOFO. Arguments as gc_ab_cas_fofo_ex (ure_host NULL = identity);
+ * *ecorr_host = ECorr, *etot_host = E_CAS w/o ENuc (may be NULL). Blocks larger
+ * than 64 pairs (nact > 11) return GC_EUNSUPPORTED. */
+int gc_ac0cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                   const double *occ_host, const double *ure_host, const double *xone_host,
+                   const int *indn_host, const double *rdm2act_host, const double *ffoo_dev,
+                   const double *fofo_dev, double *ecorr_host, double *etot_host);
+
 /* Whole lambda quadrature ------------------------------------------------ */
 
 /* ACECORR, acfd.f:117-209 with ACEInteg_FOFO, abfofo.f90:3664-3789: for each

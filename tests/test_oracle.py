@@ -174,3 +174,24 @@ def test_edge_shapes_fofo_equals_incore(cfg):
                                       ngrid=1)
     assert x[0] == pytest.approx(0.5) and w[0] == pytest.approx(1.0)
     assert abs(ecorr - w1) < 1e-12 * max(1.0, abs(w1))
+
+
+def test_ac0_oracle_is_the_first_order_connection():
+    """AC0CAS_FOFO's energy is the linearised adiabatic connection: with W(0) = 0,
+    E_AC0 = W(0) + W'(0)/2, W' from a central difference of the line-faithful
+    ACEInteg_FOFO restatement (an independent pin of the AC0 oracle)."""
+    from oracle import ac0_ref as A
+    from gammcor_gb300 import synth
+    s = synth.make_system(n=20, nin=2, nact=2, rank=80, seed=1)
+    ffoo, fofo = R.transform_fofo_ffoo(s.cmo, s.ao_eri_packed(), s.nin, s.nact)
+    indn = R.pair_space(s.occ, s.nele)
+    e0, etot = A.ac0cas_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo,
+                             s.rdm2act)
+
+    def W(lam):
+        return R.ace_integ_fofo(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act, lam)[0]
+    h = 1e-4
+    w0, wp = W(0.0), (W(h) - W(-h)) / (2 * h)
+    assert abs(w0) < 1e-12
+    assert abs(e0 - (w0 + 0.5 * wp)) < 1e-9, (e0, w0 + 0.5 * wp)
+    assert abs(etot - s.e_cas) < 1e-10
