@@ -62,6 +62,9 @@ SIGNATURES = {
     "gc_erpasymm1": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp]),
     "gc_ac0cas_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _dp,
                                  _vp, _vp, _dp, _dp]),
+    "gc_freq_grid": (C.c_int, [C.c_int, _dp, _dp]),
+    "gc_ac_freq_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _ip, _dp,
+                                  _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "gc_erpa": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int]),
     "gc_erpa_ex": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.c_int]),
     "gc_ace_ne_erpa_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,

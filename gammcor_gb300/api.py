@@ -307,6 +307,34 @@ def ac0cas_fofo(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ure=None,
     return ec.value, et.value
 
 
+def freq_grid(nfreq: int):
+    """FreqGrid (ac_iter.f:414-429): frequencies and weights of the ACFREQ integral."""
+    x = np.zeros(nfreq)
+    w = np.zeros(nfreq)
+    check(None, load().gc_freq_grid(nfreq, _dptr(x), _dptr(w)))
+    return x, w
+
+
+def ac_freq_fofo(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, nfreq: int = 25,
+                 max_cn: int = 3, precision: str = "fp64", erpa_mode: str = "cholesky", ure=None,
+                 ctx: Context | None = None):
+    """WIter_FOFO (ac_fofo.f90:1-181), the ACFREQ energy: returns (ECorr, ECASSCF)."""
+    ctx = ctx or default_context(ffoo.device.index or 0)
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    xone = np.ascontiguousarray(xone, dtype=np.float64)
+    ind = np.ascontiguousarray(indn, dtype=np.int32).ravel()
+    rdm = np.ascontiguousarray(rdm2act, dtype=np.float64)
+    u = None if ure is None else np.asfortranarray(ure, dtype=np.float64)
+    ec, et = C.c_double(), C.c_double()
+    check(ctx.h, load().gc_ac_freq_fofo(ctx.h, occ.shape[0], inactive, nact, ind.shape[0] // 2,
+                                        _dptr(occ),
+                                        _dptr(u.ravel(order="F")) if u is not None else None,
+                                        _dptr(xone), _iptr(ind), _dptr(rdm), _ptr(ffoo),
+                                        _ptr(fofo), int(nfreq), int(max_cn), PREC[precision],
+                                        ERPA[erpa_mode], C.byref(ec), C.byref(et)))
+    return ec.value, et.value
+
+
 def acecorr(occ, xone, indn, nact, inactive, ffoo, fofo, rdm2act, ngrid: int = 5,
             erpa_mode: str = "symm1", precision: str = "fp64", ctx: Context | None = None):
     """ACECORR (acfd.f:117-209). Returns (E_CAS, ECorr, [W(lambda_i)])."""

@@ -883,6 +883,44 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
 
 }  // namespace gc
 
+namespace gc {
+
+int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, double *L,
+             double *U, double *w, int mode, int prec) {
+  if (N <= 0) return set_error(ctx, GC_EINVAL, "chol_eig: N=%d", N);
+  const size_t NN = (size_t)N * N;
+  const dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
+  DevBuf<double> am;
+  GC_TRY(am.alloc(ctx, NN));
+  GC_CUDA(ctx, cudaMemcpyAsync(L, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  GC_CUDA(ctx, cudaMemcpyAsync(am.p, abmin, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, L);
+  GC_LAUNCHED(ctx);
+  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, am.p);
+  GC_LAUNCHED(ctx);
+  const bool tc = prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6;
+  int minor = 0;
+  if (tc && ctx->chol_blocked && N >= kCholBlockedMin)
+    GC_TRY(chol_blocked(ctx, N, L, prec, kCholBlock, &minor));
+  else
+    GC_TRY(chol_plain(ctx, N, L, &minor));
+  if (minor > 0)
+    return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
+  k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L);
+  GC_LAUNCHED(ctx);
+  // U <- L^T A- L (the eigenvectors overwrite it)
+  DevBuf<double> T;
+  GC_TRY(T.alloc(ctx, NN));
+  GC_TRY(product(ctx, prec, false, N, N, N, am.p, N, L, N, T.p, N));
+  GC_TRY(product(ctx, prec, true, N, N, N, L, N, T.p, N, U, N));
+  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, U);
+  GC_LAUNCHED(ctx);
+  return eigen(ctx, N, U, w, mode == GC_ERPA_CHOLESKY_REFINED ? mode : GC_ERPA_CHOLESKY, prec);
+}
+
+}  // namespace gc
+
 extern "C" int gc_erpa(gc_context *ctx, int ndimx, double *abplus, double *abmin, double *eigvec,
                        double *eig, int mode) {
   if (!ctx) return GC_EINVAL;

@@ -146,6 +146,13 @@ int rotate_h(gc_context *ctx, SysDev &sd, const double *ure_host);
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *eigvec,
                double *eig, int mode, int gemm_precision, bool aplsqrt_out = false);
 
+// A+ = L L^T (L lower, upper triangle zeroed) and the eigenpairs of L^T A- L: U (N x N,
+// column k = eigenvector k), w (eigenvalues; ascending except in the refined mode).
+// A+ and A- are read, symmetrised copies are used. mode: GC_ERPA_CHOLESKY (dsyevd) or
+// GC_ERPA_CHOLESKY_REFINED; prec: arithmetic of the products (FP64 or FP64TC5/6).
+int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, double *L,
+             double *U, double *w, int mode, int prec);
+
 // Integrand (gc_integrand.cu).
 int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,
               const double *fofo, int precision, double *w_host);

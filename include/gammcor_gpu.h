@@ -225,6 +225,28 @@ int gc_ac0cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
                    const int *indn_host, const double *rdm2act_host, const double *ffoo_dev,
                    const double *fofo_dev, double *ecorr_host, double *etot_host);
 
+/* ACFREQ ---------------------------------------------------------------------- */
+
+/* FreqGrid, ac_iter.f:414-429: nfreq Gauss-Legendre points on [-1, 1] mapped to
+ * frequencies x in [0, inf) with x0 = 1/2, and their weights w. */
+int gc_freq_grid(int nfreq, double *x, double *w);
+
+/* WIter_FOFO, ac_fofo.f90:1-181 (the ACFREQ job, ac_iter.f:44-48): the AC
+ * correlation energy from the imaginary-frequency integral of the response,
+ * expanded to order max_cn in lambda (the reference uses nfreq = 25,
+ * max_cn = 3), contracted with FOFO as the integrand is. The series is carried
+ * in the eigenbasis of the lambda = 0 ERPA problem (one Cholesky, one
+ * eigensolve of mode GC_ERPA_CHOLESKY or GC_ERPA_CHOLESKY_REFINED), so each
+ * frequency costs element-wise passes and 2 (max_cn - 2) + 1 GEMMs in the given
+ * precision (GC_PREC_FP64, GC_PREC_FP64TC5 or GC_PREC_FP64TC6) instead of an LU
+ * inverse. Needs A+B(0) positive definite (GC_ENOTPD otherwise). Other arguments
+ * as gc_ab_cas_fofo_ex; *etot_host = E_CAS w/o ENuc (may be NULL). */
+int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
+                    const double *occ_host, const double *ure_host, const double *xone_host,
+                    const int *indn_host, const double *rdm2act_host, const double *ffoo_dev,
+                    const double *fofo_dev, int nfreq, int max_cn, int precision, int erpa_mode,
+                    double *ecorr_host, double *etot_host);
+
 /* Whole lambda quadrature ------------------------------------------------ */
 
 /* ACECORR, acfd.f:117-209 with ACEInteg_FOFO, abfofo.f90:3664-3789: for each

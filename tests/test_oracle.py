@@ -195,3 +195,25 @@ def test_ac0_oracle_is_the_first_order_connection():
     assert abs(w0) < 1e-12
     assert abs(e0 - (w0 + 0.5 * wp)) < 1e-9, (e0, w0 + 0.5 * wp)
     assert abs(etot - s.e_cas) < 1e-10
+
+
+def test_acfreq_oracle_first_order_is_ac0():
+    """Truncated after the first-order term (Max_Cn = 1), the frequency integral of
+    WIter_FOFO must reproduce the AC0 energy (W(0) + W'(0)/2) once the frequency
+    grid is fine enough: an independent pin of the ACFREQ oracle's series and
+    frequency quadrature."""
+    from oracle import ac0_ref as A
+    from oracle import acfreq_ref as F
+    from gammcor_gb300 import synth
+    s = synth.make_system(n=20, nin=2, nact=2, rank=80, seed=1)
+    ffoo, fofo = R.transform_fofo_ffoo(s.cmo, s.ao_eri_packed(), s.nin, s.nact)
+    indn = R.pair_space(s.occ, s.nele)
+    e0, _ = A.ac0cas_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo, s.rdm2act)
+    e1, ecas = F.witer_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo,
+                            s.rdm2act, ngrid=120, max_cn=1)
+    assert abs(e1 - e0) < 1e-10, (e1, e0)
+    assert abs(ecas - s.e_cas) < 1e-10
+    # the reference settings (25 points, third order) stay close to the lambda quadrature
+    e3, _ = F.witer_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo, s.rdm2act)
+    eac = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act, ngrid=8)[1]
+    assert abs(e3 - eac) < 1e-3 * abs(eac)
