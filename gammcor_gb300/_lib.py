@@ -17,6 +17,7 @@ STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "
                 9: "GC_ENONFINITE"}
 PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "fp64tc5": 3, "fp64tc6": 4}
 ERPA = {"symm1": 0, "cholesky": 1, "refined": 2}
+TWOINT = {"dalton8": 0, "dalton16": 1, "pqrs": 2, "triangle": 3}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -53,6 +54,8 @@ SIGNATURES = {
     "gc_pair_space": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_double, _ip, _ip]),
     "gc_tran4_gen": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp,
                                _vp, _vp, C.c_int]),
+    "gc_sort_twoint": (C.c_int, [_vp, C.c_int, C.c_longlong, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "gc_ao_eri_factored": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_int]),
     "gc_tran4_factored": (C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int,
                                     _vp, C.c_int, _vp, _vp, C.c_int]),
     "gc_ab_cas_fofo": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _dp, _vp,

@@ -163,6 +163,37 @@ def tran4_gen(nbas: int, CA: torch.Tensor, CB: torch.Tensor, CC: torch.Tensor, C
     return out
 
 
+def readtwoint(nbas: int, values: torch.Tensor, labels: torch.Tensor | None, fmt: str,
+               out: torch.Tensor | None = None, ctx: Context | None = None) -> torch.Tensor:
+    """readtwoint (sorter.f90:31-395) for one chunk of integrals already on the device:
+    values (FP64) and labels (int32, fmt 'dalton8', 'dalton16', 'pqrs', or None for
+    'triangle'). Returns the AOTWOSORT tensor (ntr, ntr), record rs = row; pass the
+    tensor of an earlier chunk as `out` to add a further chunk."""
+    ctx = ctx or default_context(values.device.index or 0)
+    ntr = nbas * (nbas + 1) // 2
+    init = out is None
+    if out is None:
+        out = torch.empty((ntr, ntr), dtype=torch.float64, device=values.device)
+    if values.dtype != torch.float64 or (labels is not None and labels.dtype != torch.int32):
+        raise ValueError("values must be float64 and labels int32")
+    check(ctx.h, load().gc_sort_twoint(ctx.h, nbas, values.numel(), _ptr(values),
+                                       _ptr(labels) if labels is not None else None,
+                                       _lib.TWOINT[fmt], int(init), _ptr(out)))
+    return out
+
+
+def ao_eri_factored(nbas: int, lfac: torch.Tensor, precision: str = "fp64",
+                    ctx: Context | None = None) -> torch.Tensor:
+    """The AOTWOSORT tensor L L^T from the ERI factor (ntr, rank) with Fortran meaning."""
+    ctx = ctx or default_context(lfac.device.index or 0)
+    ntr = nbas * (nbas + 1) // 2
+    lcol = _fortran_cols(lfac)
+    out = torch.empty((ntr, ntr), dtype=torch.float64, device=lfac.device)
+    check(ctx.h, load().gc_ao_eri_factored(ctx.h, nbas, lfac.shape[1], _ptr(lcol), _ptr(out),
+                                           PREC[precision]))
+    return out
+
+
 def tran4_factored(nbas: int, lfac: torch.Tensor, CA, CB, CC, CD, precision: str = "fp64",
                    ctx: Context | None = None, out: torch.Tensor | None = None) -> torch.Tensor:
     """tran4_gen's output from the ERI factor; lfac is (ntr, rank) with Fortran meaning."""

@@ -123,6 +123,32 @@ int gc_tran4_gen(gc_context *ctx, int nbas,
                  int nC, const double *CC_dev, int nD, const double *CD_dev,
                  const double *ao_sorted_dev, double *out_dev, int precision);
 
+/* Label formats of the AO integral files readtwoint decodes (sorter.f90:31-395). */
+enum gc_twoint_format {
+  GC_TWOINT_DALTON8 = 0,   /* one int per integral: p, q, r, s in bits 0-7, 8-15, 16-23, 24-31 */
+  GC_TWOINT_DALTON16 = 1,  /* two ints per integral: (r | s << 16), (p | q << 16) */
+  GC_TWOINT_PQRS = 2,      /* four ints per integral: p, q, r, s */
+  GC_TWOINT_TRIANGLE = 3   /* no labels: all ntr(ntr+1)/2 values with pq >= rs, pq outer */
+};
+
+/* readtwoint, sorter.f90:31-395: one chunk of AO integrals (val_dev, labels_dev,
+ * device memory) sorted into the AOTWOSORT tensor ao_sorted_dev (ntr records of
+ * ntr doubles, record rs holds (pq|rs), pq = p + q(q-1)/2). Each integral goes to
+ * record rs at pq and, by the format's rule, to record pq at rs; a slot written
+ * twice keeps the later integral, within a chunk and across chunks (calls are
+ * ordered on the context's stream). init = 1 zeroes the tensor first, as the
+ * reference starts every record at zero. Labels outside 1..nbas are skipped and
+ * reported with GC_EINVAL after the chunk. */
+int gc_sort_twoint(gc_context *ctx, int nbas, long long nints, const double *val_dev,
+                   const int *labels_dev, int format, int init, double *ao_sorted_dev);
+
+/* The AOTWOSORT tensor from the ERI factor: (pq|rs) = sum_P L(pq,P) L(rs,P), i.e.
+ * L L^T with lfac_dev (ntr x rank, column-major), in the given precision. No
+ * counterpart routine in the reference: the on-device producer of the tensor
+ * that gc_tran4_gen reads, for inputs given as a factor. */
+int gc_ao_eri_factored(gc_context *ctx, int nbas, int rank, const double *lfac_dev,
+                       double *ao_sorted_dev, int precision);
+
 /* Same output as gc_tran4_gen from the ERI factor instead of the 4-index AO
  * tensor: (pq|rs) = sum_P L(pq,P) L(rs,P), lfac_dev = L as (ntr x rank)
  * column-major with the AOTWOSORT pair packing. No counterpart routine in the
