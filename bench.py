@@ -483,7 +483,7 @@ def run_ours(args):
     # for that are reported beside it.
     hbm, bf16, src = read_peaks()
     Nmax = max(Ns)
-    npass = {"bf16x3": 3, "bf16x6": 6, "fp64tc5": 15, "fp64tc6": 21}[args.precision]
+    npass = {"bf16x3": 3, "bf16x6": 6, "fp64tc4": 10, "fp64tc5": 15, "fp64tc6": 21}[args.precision]
     ms_k = api.tc_gemm_time(Nmax, Nmax, Nmax, args.precision, reps=5)
     ach = 2.0 * Nmax ** 3 / (ms_k / 1000.0) / 1e12
     roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",

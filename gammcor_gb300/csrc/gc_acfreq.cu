@@ -31,7 +31,7 @@ namespace {
 // C (m x n) = op(A) op(B), column-major, in the given precision.
 int gemm(gc_context *ctx, int prec, bool ta, bool tb, int m, int n, int k, const double *A, int lda,
          const double *B, int ldb, double *C, int ldc) {
-  if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6)
+  if (gc::is_sliced(prec))
     // A(m, k) = A[m * sam + k * sak]; B(n, k) = B[n * sbn + k * sbk]
     return gc::tc_gemm_strided(ctx, prec, m, n, k, A, ta ? lda : 1, ta ? 1 : lda, B, tb ? 1 : ldb,
                                tb ? ldb : 1, C, ldc);
@@ -151,7 +151,7 @@ extern "C" int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, 
                                int erpa_mode, double *ecorr, double *etot) {
   if (!ctx) return GC_EINVAL;
   if (!ecorr || !ffoo || !fofo || nfreq <= 0 || nfreq > 1000 || max_cn < 1 || max_cn > 12 ||
-      (precision != GC_PREC_FP64 && precision != GC_PREC_FP64TC5 && precision != GC_PREC_FP64TC6) ||
+      (precision != GC_PREC_FP64 && !gc::is_sliced(precision)) ||
       (erpa_mode != GC_ERPA_CHOLESKY && erpa_mode != GC_ERPA_CHOLESKY_REFINED))
     return gc::set_error(ctx, GC_EINVAL, "ac_freq_fofo: bad arguments");
   const int N = ndimx;

@@ -535,7 +535,7 @@ __global__ void k_colnorm(int N, double *__restrict__ X) {
 // B k x n, all leading dimensions equal to the row count N of the square case.
 int product(gc_context *ctx, int prec, bool transA, int m, int n, int k, const double *A,
             int lda, const double *B, int ldb, double *C, int ldc) {
-  if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6)
+  if (gc::is_sliced(prec))
     return gc::tc_gemm_strided(ctx, prec, m, n, k, A, transA ? lda : 1, transA ? 1 : lda, B, ldb,
                                1, C, ldc);
   const double one = 1.0, zero = 0.0;
@@ -615,7 +615,7 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
     GC_TRY(product(ctx, prec, false, N, N, N, M, N, X, N, P, N));        // P = M X
     // [G S] = X^T [X P]; both blocks are symmetric, so on the tensor-core path only
     // their lower triangles are computed and mirrored
-    if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6) {
+    if (gc::is_sliced(prec)) {
       GC_TRY(gc::tc_gemm_strided_lower(ctx, prec, N, 2 * N, N, X, N, 1, X, N, 1, G, N, N));
       k_mirror_lower<<<g2, b2, 0, ctx->stream>>>(N, G);
       GC_LAUNCHED(ctx);
@@ -651,7 +651,7 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
     k_eig_update<<<N, 256, 0, ctx->stream>>>(N, G, S, P, dS.p, dG.p, lam);
     GC_LAUNCHED(ctx);
     // D = E E^T into the S slot (S is no longer needed); low relative accuracy suffices
-    if (prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6) {
+    if (gc::is_sliced(prec)) {
       GC_TRY(gc::tc_gemm_nt(ctx, GC_PREC_BF16X6, N, N, N, P, N, P, N, S, N));
     } else {
       const double one = 1.0, zero = 0.0;
@@ -837,7 +837,7 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_TRY(M.alloc(ctx, NN));
     GC_CUDA(ctx, cudaMemcpyAsync(L.p, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
-    const bool tc_prec = gemm_precision == GC_PREC_FP64TC5 || gemm_precision == GC_PREC_FP64TC6;
+    const bool tc_prec = gc::is_sliced(gemm_precision);
     int minor = 0;
     if (tc_prec && ctx->chol_blocked && N >= kCholBlockedMin)
       GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, kCholBlock, &minor));
@@ -847,7 +847,7 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
       return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
     k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
     GC_LAUNCHED(ctx);
-    const bool tc = gemm_precision == GC_PREC_FP64TC5 || gemm_precision == GC_PREC_FP64TC6;
+    const bool tc = gc::is_sliced(gemm_precision);
     if (tc) {
       // T = A- L (into Y as scratch); M = L^T T; after the eigensolve Y = L U.
       // Products of the FP64-accurate sliced tensor-core GEMM (L has a zero upper triangle).
@@ -899,7 +899,7 @@ int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, 
   GC_LAUNCHED(ctx);
   k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, am.p);
   GC_LAUNCHED(ctx);
-  const bool tc = prec == GC_PREC_FP64TC5 || prec == GC_PREC_FP64TC6;
+  const bool tc = gc::is_sliced(prec);
   int minor = 0;
   if (tc && ctx->chol_blocked && N >= kCholBlockedMin)
     GC_TRY(chol_blocked(ctx, N, L, prec, kCholBlock, &minor));
@@ -931,7 +931,7 @@ extern "C" int gc_erpa(gc_context *ctx, int ndimx, double *abplus, double *abmin
 extern "C" int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus, double *abmin,
                           double *eigvec, double *eig, int mode, int precision) {
   if (!ctx) return GC_EINVAL;
-  if (precision != GC_PREC_FP64 && precision != GC_PREC_FP64TC5 && precision != GC_PREC_FP64TC6)
+  if (precision != GC_PREC_FP64 && !gc::is_sliced(precision))
     return gc::set_error(ctx, GC_EINVAL, "gc_erpa_ex: precision %d is not FP64-accurate", precision);
   GC_TRY(gc::erpa_solve(ctx, ndimx, abplus, abmin, eigvec, eig, mode, precision));
   return gc::check_flag(ctx);

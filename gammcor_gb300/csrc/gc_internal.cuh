@@ -117,6 +117,12 @@ struct DevBuf {
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 
+// The FP64-accurate sliced tensor-core precisions (4, 5 or 6 integer BF16 slices).
+inline bool is_sliced(int precision) {
+  return precision == GC_PREC_FP64TC4 || precision == GC_PREC_FP64TC5 ||
+         precision == GC_PREC_FP64TC6;
+}
+
 // Per-system description resident on the device ------------------------------
 struct SysDev {
   int n = 0, nin = 0, nact = 0, nocc = 0, ndimx = 0;

@@ -796,11 +796,11 @@ struct OzOperand {
   int rows = 0, Kp = 0, nb = 1, S = 0;
 };
 
-bool is_oz(int precision) { return precision == GC_PREC_FP64TC5 || precision == GC_PREC_FP64TC6; }
+bool is_oz(int precision) { return gc::is_sliced(precision); }
 
 OzPlan oz_plan(int precision) {
   OzPlan p{};
-  p.S = precision == GC_PREC_FP64TC6 ? 6 : 5;
+  p.S = precision == GC_PREC_FP64TC6 ? 6 : (precision == GC_PREC_FP64TC4 ? 4 : 5);
   int n = 0;
   for (int d = 0; d < p.S; ++d)
     for (int t = 0; t <= d; ++t) {
@@ -886,8 +886,9 @@ int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N
   epi.eb = B.exps.p;
   epi.ea_sb = A.nb > 1 ? A.rows : 0;
   epi.eb_sb = B.nb > 1 ? B.rows : 0;
-  return pl.S == 6 ? launch_oz<6>(ctx, A, B, M, N, nbatch, pl, epi)
-                   : launch_oz<5>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 6) return launch_oz<6>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 4) return launch_oz<4>(ctx, A, B, M, N, nbatch, pl, epi);
+  return launch_oz<5>(ctx, A, B, M, N, nbatch, pl, epi);
 }
 
 }  // namespace

@@ -113,7 +113,7 @@ extern "C" int gc_tran4_gen(gc_context *ctx, int nbas, int nA, const double *CA,
                             const double *G, double *out, int precision) {
   if (!ctx) return GC_EINVAL;
   GC_TRY(check_dims(ctx, nbas, nA, nB, nC, nD));
-  if (precision < GC_PREC_FP64 || precision > GC_PREC_FP64TC6)
+  if (precision < GC_PREC_FP64 || precision > GC_PREC_FP64TC4)
     return gc::set_error(ctx, GC_EINVAL, "tran4_gen: unknown precision %d", precision);
   const int n = nbas;
   const long long ntr = (long long)n * (n + 1) / 2;

@@ -43,7 +43,9 @@ enum gc_precision {
                           5 integer BF16 slices; products of equal weight accumulate exactly in
                           FP32 over K chunks short enough to stay below 2^24; chunks summed in
                           FP64. 15 passes, error ~2^-35 of |A||B|^T */
-  GC_PREC_FP64TC6 = 4  /* as FP64TC5 with 6 slices: 21 passes, error ~2^-42 of |A||B|^T */
+  GC_PREC_FP64TC6 = 4, /* as FP64TC5 with 6 slices: 21 passes, error ~2^-42 of |A||B|^T */
+  GC_PREC_FP64TC4 = 5  /* as FP64TC5 with 4 slices: 10 passes, error ~2^-28 of |A||B|^T
+                          (between FP32 and FP64) */
 };
 
 /* ERPA eigen-solver form. */
@@ -203,7 +205,7 @@ int gc_erpa(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
             double *eigvec_dev, double *eig_dev, int mode);
 /* gc_erpa with the arithmetic of the Cholesky form's matrix products (and of the
  * refinement products of GC_ERPA_CHOLESKY_REFINED) chosen by precision: GC_PREC_FP64
- * (cuBLAS) or GC_PREC_FP64TC5 / GC_PREC_FP64TC6 (sliced tensor-core GEMM). The
+ * (cuBLAS) or GC_PREC_FP64TC4 / 5 / 6 (sliced tensor-core GEMM). The
  * eigenvalues of the refined mode are not sorted. */
 int gc_erpa_ex(gc_context *ctx, int ndimx, double *abplus_dev, double *abmin_dev,
                double *eigvec_dev, double *eig_dev, int mode, int precision);
@@ -264,7 +266,7 @@ int gc_freq_grid(int nfreq, double *x, double *w);
  * in the eigenbasis of the lambda = 0 ERPA problem (one Cholesky, one
  * eigensolve of mode GC_ERPA_CHOLESKY or GC_ERPA_CHOLESKY_REFINED), so each
  * frequency costs element-wise passes and 2 (max_cn - 2) + 1 GEMMs in the given
- * precision (GC_PREC_FP64, GC_PREC_FP64TC5 or GC_PREC_FP64TC6) instead of an LU
+ * precision (GC_PREC_FP64 or a sliced GC_PREC_FP64TC4/5/6) instead of an LU
  * inverse. Needs A+B(0) positive definite (GC_ENOTPD otherwise). Other arguments
  * as gc_ab_cas_fofo_ex; *etot_host = E_CAS w/o ENuc (may be NULL). */
 int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
