@@ -338,6 +338,7 @@ constexpr int OZ_MAXS = 6;
 constexpr int kBadExp = 0x7fffffff;
 
 constexpr int OZ_EPI_WARPS = 8;                   // two per TMEM lane quarter
+constexpr int OZ_GROUP_M = 8;                     // row tiles per raster group
 constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;  // TMA warp, MMA warp, epilogue
 
 struct OzPlan {
@@ -384,7 +385,22 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   __shared__ double red[OZ_EPI_WARPS];
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * OZ_BN, b = blockIdx.z;
+  // Grouped raster: CTAs are scheduled roughly in linear order, so consecutive ones
+  // take OZ_GROUP_M row tiles before moving to the next column tile. A wave of CTAs
+  // then shares a few A and B panels in L2 instead of sweeping every A panel
+  // (which does not fit in L2 at large M) once per column tile.
+  int mt, nt;
+  {
+    const int ntm = gridDim.x, ntn = gridDim.y;
+    const long long t = blockIdx.x + (long long)ntm * blockIdx.y;
+    const long long per_group = (long long)OZ_GROUP_M * ntn;
+    const int first_m = (int)(t / per_group) * OZ_GROUP_M;
+    const int gm = min(ntm - first_m, OZ_GROUP_M);
+    const int r = (int)(t % per_group);
+    mt = first_m + r % gm;
+    nt = r / gm;
+  }
+  const int m0 = mt * BM, n0 = nt * OZ_BN, b = blockIdx.z;
   const int nchunks = (kblocks + plan.chunk_kb - 1) / plan.chunk_kb;
   if (epi.tri_period > 0) {  // whole CTA, before any barrier or TMEM is set up
     const int c0 = n0 % epi.tri_period;
