@@ -70,6 +70,9 @@ def parse():
                     help="input generator: FP64 torch on the GPU, or numpy on the host")
     ap.add_argument("--no-subset", action="store_true",
                     help="skip the plain FP64 GPU path on the whole batch (comparison and check)")
+    ap.add_argument("--plain-energies", default=None,
+                    help="file of the plain FP64 energies of this batch: read when it exists "
+                         "(the check runs without the plain timing), written otherwise")
     ap.add_argument("--kernel-only", type=int, default=0,
                     help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -83,6 +86,10 @@ def parse():
     ap.add_argument("--erpa-once", action="store_true",
                     help="time one ERPA solve (the --erpa form) of the largest batch system, "
                          "inside a profiler range (for profiling)")
+    ap.add_argument("--acecorr-once", action="store_true",
+                    help="one ACECORR point (A+-B assembly at lambda = 0 and 1, ERPA, integrand) "
+                         "of the largest batch system inside a profiler range (for profiling the "
+                         "assembly and integrand kernels)")
     return ap.parse_args()
 
 
@@ -352,7 +359,7 @@ def run_ours(args):
     __graft_entry__.build()
     from gammcor_gb300 import api, surrogate
 
-    if args.erpa_once:
+    if args.erpa_once or args.acecorr_once:
         from gammcor_gb300 import synth
         shapes = synth.batched_shapes(args.nsys, args.seed)
 
@@ -368,6 +375,23 @@ def run_ours(args):
         indn = api.pair_space(s.occ, s.nele)
         fofo = api.tran4_factored(s.n, L, C, co, C, co, precision=args.precision)
         ffoo = api.tran4_factored(s.n, L, co, co, C, C, precision=args.precision)
+        if args.acecorr_once:
+            run = lambda: api.acecorr(s.occ, s.xone, indn, s.nact, s.nin, ffoo, fofo,  # noqa: E731
+                                      s.rdm2act, ngrid=1, erpa_mode=args.erpa,
+                                      precision=args.precision)
+            run()  # warm-up
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.cudart().cudaProfilerStart()
+            e0.record()
+            run()
+            e1.record()
+            torch.cuda.synchronize()
+            torch.cuda.cudart().cudaProfilerStop()
+            print(json.dumps({"acecorr_point": args.erpa, "precision": args.precision,
+                              "N": len(indn), "n": s.n, "nocc": s.nocc,
+                              "ms": e0.elapsed_time(e1)}))
+            return
         abp, abm, _ = api.ab_cas_fofo(s.occ, s.xone, indn, s.nact, s.nin, ffoo, fofo, s.rdm2act, 0.5)
         api.erpasymm1(abp.clone(), abm.clone(), mode=args.erpa, precision=args.precision)  # warm-up
         torch.cuda.synchronize()
@@ -467,7 +491,11 @@ def run_ours(args):
     # point) on the whole batch with the same worker streams, timed with CUDA events; every
     # energy of the last timed step is checked against it.
     plain = None
-    if not args.no_subset:
+    cached = args.plain_energies and Path(args.plain_energies).exists()
+    if not args.no_subset and cached:
+        d = np.load(args.plain_energies)
+        pe, pst, t_plain, pclk = d["ecorr"], d["status"], float(d["ms"]), None
+    elif not args.no_subset:
         pl = dict(ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
                   nstreams=args.nstreams)
         torch.cuda.synchronize()
@@ -478,14 +506,21 @@ def run_ours(args):
             p1.record(stream)
             torch.cuda.synchronize()
         t_plain = p0.elapsed_time(p1)
+        if args.plain_energies:
+            np.savez(args.plain_energies, ecorr=pe, status=pst, ms=t_plain)
+    if not args.no_subset:
         good = (pst == 0) & (status == 0)
         err = np.abs(ecorr - pe)[good]
+        worst = int(np.nonzero(good)[0][np.argmax(err)]) if err.size else None
         plain = {"systems": int(good.sum()), "plain_ms": t_plain, "step_ms": ms,
+                 "worst_system": worst, "worst_ndimx": Ns[worst] if worst is not None else None,
+                 "median_abs_err_eh": float(np.median(err)) if err.size else None,
                  "speedup": t_plain / ms, "streams": args.nstreams,
                  "max_abs_err_eh": float(err.max()) if err.size else None,
                  "within_1ueh": bool(err.size and err.max() <= 1e-6),
-                 "timing": "CUDA events on the calling stream, whole batch",
-                 "clocks": pclk.summary()}
+                 "timing": ("CUDA events on the calling stream, whole batch" +
+                            (" (energies and time read from an earlier run)" if cached else "")),
+                 "clocks": pclk.summary() if pclk else None}
         log(f"plain FP64 on all {int(good.sum())} systems: {t_plain / 1000:.1f}s vs step "
             f"{ms / 1000:.1f}s ({t_plain / ms:.2f}x), max |dE| {plain['max_abs_err_eh']:.2e}")
 

@@ -185,8 +185,11 @@ int gc_acecorr(gc_context *ctx, int nbas, int ninact, int nact, int ndimx, const
   if (!ctx) return GC_EINVAL;
   if (ngrid <= 0 || ngrid > 100 || !xone || !ffoo || !fofo || !ecorr || !ecas)
     return gc::set_error(ctx, GC_EINVAL, "acecorr: bad arguments (ngrid=%d)", ngrid);
+  if (!indn) return gc::set_error(ctx, GC_EINVAL, "acecorr: null IndN");
   gc::SysDev sd;
-  GC_TRY(gc::sys_upload(ctx, sd, nbas, ninact, nact, ndimx, occ, xone, indn, rdm2act));
+  // pairs in the coalescing order (the energies do not depend on the pair order)
+  const std::vector<int> ind = gc::coalesced_pair_order(indn, ndimx);
+  GC_TRY(gc::sys_upload(ctx, sd, nbas, ninact, nact, ndimx, occ, xone, ind.data(), rdm2act));
   std::vector<double> x(ngrid), w(ngrid);
   gc_gauleg(0.0, 1.0, x.data(), w.data(), ngrid);
   const size_t NN = (size_t)ndimx * ndimx;

@@ -93,7 +93,8 @@ __global__ void k_wmat(Geo g, const int *__restrict__ grp, const double *__restr
       for (int j = 0; j < g.nocc; ++j) {
         int gj = grp[j];
         for (int i = 0; i < g.nocc; ++i)
-          s += AC(g, gk, gl, grp[i], gj, lam) * Fofo(fofo, g, k, l, i, j) * RV(rv, g.nocc, i, j, r, l);
+          // (kl|ij) read as (ij|kl): consecutive k are consecutive elements of record (i, j)
+          s += AC(g, gk, gl, grp[i], gj, lam) * Fofo(fofo, g, i, j, k, l) * RV(rv, g.nocc, i, j, r, l);
       }
     }
   }
@@ -143,13 +144,14 @@ __global__ void k_z1(Geo g, const double *__restrict__ fofo, const double *__res
     double s = 0.0;
     for (int u = 0; u < g.nact; ++u)
       for (int tt = 0; tt < g.nact; ++tt)
-        s += Fofo(fofo, g, a, b, g.nin + tt, g.nin + u) *
+        s += Fofo(fofo, g, g.nin + tt, g.nin + u, a, b) *  // (ab|TU) as (TU|ab): coalesced in a
              RV(rv, g.nocc, g.nin + tt, g.nin + u, g.nin + c, g.nin + d);
     z[t] = s;
   }
 }
 
-// Z4[r,p,q,s] = sum_tu (rU|pT) RV[T,Q,S,U];  Z7[r,p,q,s] = sum_tu (rU|pT) RV[T,Q,U,S].
+// Z4[p,r,q,s] = sum_tu (rU|pT) RV[T,Q,S,U];  Z7[p,r,q,s] = sum_tu (rU|pT) RV[T,Q,U,S]
+// (p fastest, so that the element kernel reads them along consecutive p).
 __global__ void k_z47(Geo g, const double *__restrict__ fofo, const double *__restrict__ rv,
                       double *__restrict__ z4, double *__restrict__ z7) {
   size_t total = (size_t)g.n * g.n * g.nact * g.nact;
@@ -168,7 +170,7 @@ __global__ void k_z47(Geo g, const double *__restrict__ fofo, const double *__re
         a4 += f * RV(rv, g.nocc, g.nin + tt, Q, S, g.nin + u);
         a7 += f * RV(rv, g.nocc, g.nin + tt, Q, g.nin + u, S);
       }
-    size_t o = r + (size_t)g.n * (p + (size_t)g.n * (q + (size_t)g.nact * s));
+    size_t o = p + (size_t)g.n * (r + (size_t)g.n * (q + (size_t)g.nact * s));
     z4[o] = a4;
     z7[o] = a7;
   }
@@ -189,7 +191,7 @@ __global__ void k_z56(Geo g, const double *__restrict__ fofo, const double *__re
     double a5 = 0.0, a6 = 0.0;
     for (int u = 0; u < g.nact; ++u)
       for (int tt = 0; tt < g.nact; ++tt) {
-        double f = Fofo(fofo, g, r, g.nin + u, g.nin + tt, q);
+        double f = Fofo(fofo, g, g.nin + tt, q, r, g.nin + u);  // (rU|Tq) as (Tq|rU)
         a5 += f * RV(rv, g.nocc, g.nin + tt, P, S, g.nin + u);
         a6 += f * RV(rv, g.nocc, g.nin + tt, P, g.nin + u, S);
       }
@@ -198,8 +200,8 @@ __global__ void k_z56(Geo g, const double *__restrict__ fofo, const double *__re
   }
 }
 
-// Z8[q,s,p,r] = sum_tu (TU|qs) RV[T,U,P,R];  q,s < nocc.
-__global__ void k_z8(Geo g, const double *__restrict__ ffoo, const double *__restrict__ rv,
+// Z8[q,s,p,r] = sum_tu (TU|qs) RV[T,U,P,R];  q,s < nocc (read from FOFO record (T,U)).
+__global__ void k_z8(Geo g, const double *__restrict__ fofo, const double *__restrict__ rv,
                      double *__restrict__ z) {
   size_t total = (size_t)g.nocc * g.nocc * g.nact * g.nact;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
@@ -212,7 +214,7 @@ __global__ void k_z8(Geo g, const double *__restrict__ ffoo, const double *__res
     double a = 0.0;
     for (int u = 0; u < g.nact; ++u)
       for (int tt = 0; tt < g.nact; ++tt)
-        a += Ffoo(ffoo, g, g.nin + tt, g.nin + u, q, s) *
+        a += Fofo(fofo, g, g.nin + tt, g.nin + u, q, s) *  // (TU|qs) from FOFO: coalesced in q
              RV(rv, g.nocc, g.nin + tt, g.nin + u, g.nin + p, g.nin + r);
     z[t] = a;
   }
@@ -253,7 +255,7 @@ __global__ void k_z1013(Geo g, const double *__restrict__ ffoo, const double *__
     double a10 = 0.0, a13 = 0.0;
     for (int u = 0; u < g.nact; ++u)
       for (int tt = 0; tt < g.nact; ++tt) {
-        double f = Ffoo(ffoo, g, g.nin + tt, q, s, g.nin + u);
+        double f = Ffoo(ffoo, g, q, g.nin + tt, s, g.nin + u);  // (Tq|sU) as (qT|sU)
         a10 += f * RV(rv, g.nocc, g.nin + tt, P, R, g.nin + u);
         a13 += f * RV(rv, g.nocc, g.nin + tt, P, g.nin + u, R);
       }
@@ -277,7 +279,7 @@ __global__ void k_z1112(Geo g, const double *__restrict__ ffoo, const double *__
     double a11 = 0.0, a12 = 0.0;
     for (int u = 0; u < g.nact; ++u)
       for (int tt = 0; tt < g.nact; ++tt) {
-        double f = Ffoo(ffoo, g, g.nin + tt, p, s, g.nin + u);
+        double f = Ffoo(ffoo, g, p, g.nin + tt, s, g.nin + u);  // (Tp|sU) as (pT|sU)
         a11 += f * RV(rv, g.nocc, g.nin + tt, Q, R, g.nin + u);
         a12 += f * RV(rv, g.nocc, g.nin + tt, Q, g.nin + u, R);
       }
@@ -313,8 +315,9 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   if (r >= nin && p >= nin) {
     // FOFO Coulomb: A- += 4 AC X1 (rs|pq) (its two A+ parts cancel)
     vm += 4.0 * ac * X1 * Fofo(fofo, g, r, s, p, q);
-    // FOFO exchange: AC X1 (ps|rq)
-    v = ac * X1 * Fofo(fofo, g, p, s, r, q);
+    // FOFO exchange: AC X1 (ps|rq), read as (rq|ps): record (r, q) is shared by a warp
+    // of consecutive p and its elements p + s n are contiguous
+    v = ac * X1 * Fofo(fofo, g, r, q, p, s);
     vp += v;
     vm -= v;
     // FFOO exchange: -AC X1 (pr|qs)
@@ -338,7 +341,7 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   }
   if (r >= nin && sa) {
     if (qa && p >= nin) {
-      size_t o = r + (size_t)n * (p + (size_t)n * (qA + (size_t)na * sA));
+      size_t o = p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA));
       double c = AC(g, gp, gr, 1, 1, lam);
       v = c * Z.z4[o];  // T4
       vp += v;
@@ -432,6 +435,22 @@ __global__ void k_sym_avg(int N, double *__restrict__ a) {
 }  // namespace
 
 namespace gc {
+
+std::vector<int> coalesced_pair_order(const int *indn, int ndimx) {
+  if (!indn || ndimx <= 0) return {};
+  std::vector<int> idx(ndimx);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) {
+    const int qa = indn[2 * a + 1], qb = indn[2 * b + 1];
+    return qa != qb ? qa < qb : indn[2 * a] < indn[2 * b];
+  });
+  std::vector<int> out(2 * (size_t)ndimx);
+  for (int k = 0; k < ndimx; ++k) {
+    out[2 * k] = indn[2 * idx[k]];
+    out[2 * k + 1] = indn[2 * idx[k] + 1];
+  }
+  return out;
+}
 
 int rotate_h(gc_context *ctx, SysDev &sd, const double *ure_host) {
   // HNO = URe . h . URe^T, then sq_symmetrize (abfofo.f90:97-100)
@@ -561,7 +580,7 @@ static int build_z(gc_context *ctx, const SysDev &sd, const double *ffoo, const 
   GC_LAUNCHED(ctx);
   k_z56<<<grid(s1), 256, 0, ctx->stream>>>(g, fofo, sd.rv.p, Zb.z5.p, Zb.z6.p);
   GC_LAUNCHED(ctx);
-  k_z8<<<grid(s8), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z8.p);
+  k_z8<<<grid(s8), 256, 0, ctx->stream>>>(g, fofo, sd.rv.p, Zb.z8.p);
   GC_LAUNCHED(ctx);
   k_z9<<<grid(s4), 256, 0, ctx->stream>>>(g, ffoo, sd.rv.p, Zb.z9.p);
   GC_LAUNCHED(ctx);

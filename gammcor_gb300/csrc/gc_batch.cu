@@ -75,7 +75,9 @@ int build_state(gc_context *ctx, const gc_system &s, const gc_ac_params &par, Sy
                            par.precision));
   GC_TRY(gc_tran4_factored(ctx, n, s.rank, s.lfac_dev, nocc, C, nocc, C, n, C, n, C, st.ffoo.p,
                            par.precision));
-  GC_TRY(gc::sys_upload(ctx, st.sd, n, s.ninact, s.nact, N, s.occ, s.xone, s.indn, s.rdm2act));
+  // pairs in the coalescing order (the energies do not depend on the pair order)
+  const std::vector<int> ind = gc::coalesced_pair_order(s.indn, N);
+  GC_TRY(gc::sys_upload(ctx, st.sd, n, s.ninact, s.nact, N, s.occ, s.xone, ind.data(), s.rdm2act));
   if (par.affine) {
     GC_TRY(st.a0p.alloc(ctx, NN));
     GC_TRY(st.a0m.alloc(ctx, NN));

@@ -9,6 +9,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <algorithm>
+#include <numeric>
 #include <vector>
 
 #include "../../include/gammcor_gpu.h"
@@ -133,6 +135,12 @@ struct SysDev {
   DevBuf<double> h;        // (n, n) symmetrised one-electron MO matrix
   DevBuf<double> rv;       // RDM2val (nocc^4), RV[i + nocc*(j + nocc*(k + nocc*l))]
 };
+
+// IndN (2 x N, 1-based) reordered with q outer and p inner: consecutive pairs then
+// address consecutive elements p + q n of a FOFO record, so the element kernels'
+// gathers are coalesced. A+-B, the ERPA problem and W are invariant under a common
+// permutation of the pairs, so paths that return only energies may use this order.
+std::vector<int> coalesced_pair_order(const int *indn, int ndimx);
 
 // Host-side setup of SysDev (pairs, groups, RDM2val).
 int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int ndimx,

@@ -167,7 +167,7 @@ int cpu_ab_cas_fofo(int n, int nin, int nact, int N, const double *occ, const do
                 a4 += f * RVX(nin + t, nin + q, nin + s_, nin + u);
                 a7 += f * RVX(nin + t, nin + q, nin + u, nin + s_);
               }
-            const size_t o = r + (size_t)n * (p + (size_t)n * (q + (size_t)na * s_));
+            const size_t o = p + (size_t)n * (r + (size_t)n * (q + (size_t)na * s_));
             z4[o] = a4;
             z7[o] = a7;
           }
@@ -267,7 +267,7 @@ int cpu_ab_cas_fofo(int n, int nin, int nact, int N, const double *occ, const do
       }
       if (r >= nin && sa) {
         if (qa && p >= nin) {
-          const size_t o = r + (size_t)n * (p + (size_t)n * (qA + (size_t)na * sA));
+          const size_t o = p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA));
           const double c = AC(gp, gr, 1, 1, lam);
           v = c * z4[o];
           vp += v;
