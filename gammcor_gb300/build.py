@@ -18,7 +18,10 @@ CSRC = HERE / "csrc"
 OUT = HERE / "libgammcor_gpu.so"
 OBJ = HERE / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# host code without FMA contraction, so that host arithmetic (Gauss-Legendre nodes,
+# frequency grid) gives the same bits on x86-64 and aarch64 hosts
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

@@ -3,7 +3,7 @@
 
 Tolerances: 1e-9 Eh with FP64 products; 5e-9 Eh with the FP64TC5 sliced
 products and the refined eigensolve. The frequency grid matches FreqGrid to
-1e-15."""
+1e-13 relative."""
 import numpy as np
 import pytest
 import torch
@@ -24,8 +24,9 @@ def test_freq_grid(gpu_lib):
     for nf in (1, 18, 25):
         x, w = api.freq_grid(nf)
         xr, wr = F.freq_grid(nf)
-        np.testing.assert_allclose(x, xr, rtol=1e-15, atol=1e-15)
-        np.testing.assert_allclose(w, wr, rtol=1e-14, atol=1e-15)
+        # x0 (1 + x) / (1 - x) amplifies the nodes' last bits by 1 / (1 - x) near x = 1
+        np.testing.assert_allclose(x, xr, rtol=1e-13, atol=1e-15)
+        np.testing.assert_allclose(w, wr, rtol=1e-12, atol=1e-15)
 
 
 @pytest.mark.parametrize("n,nin,nact,seed", [(16, 2, 4, 0), (20, 2, 2, 1), (24, 3, 4, 3)])
