@@ -16,7 +16,7 @@ STATUS_NAMES = {0: "GC_OK", 1: "GC_EINVAL", 2: "GC_ECUDA", 3: "GC_ECUBLAS", 4: "
                 5: "GC_ENOTPD", 6: "GC_ETIMEOUT", 7: "GC_ENOMEM", 8: "GC_EUNSUPPORTED",
                 9: "GC_ENONFINITE"}
 PREC = {"fp64": 0, "bf16x3": 1, "bf16x6": 2, "fp64tc5": 3, "fp64tc6": 4, "fp64tc4": 5}
-ERPA = {"symm1": 0, "cholesky": 1, "refined": 2}
+ERPA = {"symm1": 0, "cholesky": 1, "refined": 2, "vec": 3}
 TWOINT = {"dalton8": 0, "dalton16": 1, "pqrs": 2, "triangle": 3}
 
 _dp = C.POINTER(C.c_double)

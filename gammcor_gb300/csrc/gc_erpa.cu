@@ -792,6 +792,7 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     if (bad)
       return set_error(ctx, GC_ENONFINITE, "erpa: %d non-finite elements in A+B / A-B", bad);
   }
+  if (mode == GC_ERPA_VEC) return erpavec(ctx, N, abplus, abmin, Y, eig);
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
   k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abplus);
   GC_LAUNCHED(ctx);

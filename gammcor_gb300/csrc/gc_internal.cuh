@@ -167,6 +167,9 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *ei
 int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, double *L,
              double *U, double *w, int mode, int prec);
 
+// ERPAVEC (gc_erpavec.cu): A+- symmetrised in place, Y (N x N) and omega (N).
+int erpavec(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig);
+
 // Integrand (gc_integrand.cu).
 int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,
               const double *fofo, int precision, double *w_host);

@@ -52,13 +52,17 @@ enum gc_precision {
 enum gc_erpa_mode {
   GC_ERPA_SYMM1 = 0,     /* ERPASYMM1: eig(A+), A+^1/2 A- A+^1/2, eig  (2 eigensolves) */
   GC_ERPA_CHOLESKY = 1,  /* A+ = L L^T, eig(L^T A- L), Y = L u / sqrt(2 w) (1 eigensolve) */
-  GC_ERPA_CHOLESKY_REFINED = 2 /* as GC_ERPA_CHOLESKY, with the eigensolve of L^T A- L done in
+  GC_ERPA_CHOLESKY_REFINED = 2, /* as GC_ERPA_CHOLESKY, with the eigensolve of L^T A- L done in
                           FP32 (ssyevd) and refined to FP64 accuracy: per iteration the Rayleigh
                           matrices S = X^T M X and G = X^T X in the GEMM precision, clusters of
                           close eigenvalues diagonalised exactly in FP64, and the update
                           X <- X (I + E - E E^T / 2) with E first order in the residual for the
                           rest. Falls back to dsyevd when a cluster is wider than 64 or a block
                           is singular */
+  GC_ERPA_VEC = 3        /* ERPAVEC (interpa.f:962-1070), the solver of state-averaged references
+                          (NoSt > 1): right eigenvectors of A+ A- (general FP64 eigensolver),
+                          degenerate groups orthonormalised, complex modes dropped, modes of
+                          negative norm returned with -omega; A+B need not be positive definite */
 };
 
 /* Context ------------------------------------------------------------- */

@@ -217,3 +217,20 @@ def test_acfreq_oracle_first_order_is_ac0():
     e3, _ = F.witer_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo, s.rdm2act)
     eac = R.acecorr(s.occ, s.xone, indn, s.nin, s.nact, ffoo, fofo, s.rdm2act, ngrid=8)[1]
     assert abs(e3 - eac) < 1e-3 * abs(eac)
+
+
+def test_erpavec_oracle_equals_erpasymm1_for_positive_definite_a_plus():
+    """ERPAVEC (interpa.f:962-1070) and ERPASYMM1 give the same W(lambda) when A+B
+    is positive definite: the pin of the ERPAVEC restatement."""
+    from oracle import erpavec_ref as V
+    s = small_system(n=16, nin=2, nact=4, rank=64, seed=0)
+    G, ffoo, fofo = oracle_integrals(s)
+    indn = R.pair_space(s.occ, s.nele)
+    for lam in (0.3, 0.9):
+        abp, abm, _ = R.ab_cas_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo,
+                                    s.rdm2act, lam)
+        Y1, e1, _ = R.erpasymm1(abp, abm)
+        Y2, e2 = V.erpavec(abp, abm)
+        w1 = R.ac_ene_erpa_fofo(Y1, e1, s.occ, s.nin, s.nact, indn, fofo)
+        w2 = R.ac_ene_erpa_fofo(Y2, e2, s.occ, s.nin, s.nact, indn, fofo)
+        assert abs(w1 - w2) < 1e-11
