@@ -84,6 +84,24 @@ __global__ void k_freq_xn(size_t NN, int N, double om2, int nord, const double *
   }
 }
 
+// out = x + d I
+__global__ void k_add_diag(size_t NN, int N, const double *__restrict__ x, double d,
+                           double *__restrict__ out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < NN;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(e / N), i = (int)(e - (size_t)j * N);
+    out[e] = x[e] + (i == j ? d : 0.0);
+  }
+}
+
+// out = a x + b y (element-wise)
+__global__ void k_lincomb(size_t NN, double a, const double *__restrict__ x, double b,
+                          const double *__restrict__ y, double *__restrict__ out) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < NN;
+       e += (size_t)gridDim.x * blockDim.x)
+    out[e] = a * x[e] + (y ? b * y[e] : 0.0);
+}
+
 __device__ __forceinline__ double cicoef(double o) { return o >= 0.5 ? sqrt(o) : -sqrt(o); }
 
 // ECorr partials: sum over pairs i = (p, q), j = (r, s) not in one group of
@@ -130,6 +148,86 @@ __global__ void k_sum_parts(size_t cnt, const double *__restrict__ part, double 
   if (threadIdx.x == 0) out[0] = red[0];
 }
 
+// COM of WIter_FOFO in the reference's own form (ac_fofo.f90:55-119): the inverse of
+// A0 + omega^2 by LU at every frequency (dgetrf, dgetrs on the identity) and the series
+// with FP64 products. The path when A+B(0) is not positive definite, where the
+// eigenbasis form has no Cholesky factor.
+int freq_com_lu(gc_context *ctx, int N, const double *a0p, const double *a0m, const double *a1p,
+                const double *a1m, int nfreq, int max_cn, double *com) {
+  const size_t NN = (size_t)N * N;
+  gc::DevBuf<double> A0, A1, A2, Wm, inv, C0, C1, C2, w0, w1, work;
+  for (auto *b : {&A0, &A1, &A2, &Wm, &inv, &C0, &C1, &C2, &w0, &w1}) GC_TRY(b->alloc(ctx, NN));
+  gc::DevBuf<int> ipiv;
+  GC_TRY(ipiv.alloc(ctx, N));
+  const double one = 1.0, zero = 0.0;
+  auto mm = [&](const double *A, const double *B, double *C, double alpha, double beta) {
+    return cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, &alpha, A, N, B, N, &beta, C,
+                       N);
+  };
+  GC_CUBLAS(ctx, mm(a0p, a0m, A0.p, one, zero));   // A0 = A+0 A-0
+  GC_CUBLAS(ctx, mm(a0p, a1m, A1.p, one, zero));   // A1 = A+0 A-1 + A+1 A-0
+  GC_CUBLAS(ctx, mm(a1p, a0m, A1.p, one, one));
+  GC_CUBLAS(ctx, mm(a1p, a1m, A2.p, one, zero));   // A2 = A+1 A-1
+  int lw = 0;
+  GC_CUSOLVER(ctx, cusolverDnDgetrf_bufferSize(ctx->cusolver, N, N, Wm.p, N, &lw));
+  GC_TRY(work.alloc(ctx, std::max(lw, 1)));
+  std::vector<double> xf(nfreq), wf(nfreq);
+  GC_TRY(gc_freq_grid(nfreq, xf.data(), wf.data()));
+  const double pi = 4.0 * std::atan(1.0);
+  const unsigned ew = std::min<unsigned>(gc::ceil_div(NN, 256), 152u * 16u);
+  GC_CUDA(ctx, cudaMemsetAsync(com, 0, NN * sizeof(double), ctx->stream));
+  std::vector<int> infos;
+  gc::DevBuf<int> dinfo;
+  GC_TRY(dinfo.alloc(ctx, nfreq));
+  for (int k = 0; k < nfreq; ++k) {
+    k_add_diag<<<ew, 256, 0, ctx->stream>>>(NN, N, A0.p, xf[k] * xf[k], Wm.p);
+    GC_LAUNCHED(ctx);
+    GC_CUSOLVER(ctx, cusolverDnDgetrf(ctx->cusolver, N, N, Wm.p, N, work.p, ipiv.p, dinfo.p + k));
+    GC_CUDA(ctx, cudaMemsetAsync(inv.p, 0, NN * sizeof(double), ctx->stream));
+    k_add_diag<<<ew, 256, 0, ctx->stream>>>(NN, N, inv.p, 1.0, inv.p);  // identity
+    GC_LAUNCHED(ctx);
+    GC_CUSOLVER(ctx, cusolverDnDgetrs(ctx->cusolver, CUBLAS_OP_N, N, N, Wm.p, N, ipiv.p, inv.p, N,
+                                      dinfo.p + k));
+    const double wfact = 4.0 / pi * wf[k];
+    GC_CUBLAS(ctx, mm(inv.p, a0p, C0.p, 0.5, zero));       // C0 = inv A+0 / 2
+    GC_CUBLAS(ctx, mm(inv.p, A1.p, w0.p, one, zero));      // inv A1
+    GC_CUBLAS(ctx, mm(w0.p, C0.p, C1.p, one, zero));       // C1 = inv A+1 / 2 - inv A1 C0
+    GC_CUBLAS(ctx, mm(inv.p, a1p, C1.p, 0.5, -1.0));
+    GC_CUBLAS(ctx, mm(inv.p, A2.p, w1.p, one, zero));      // inv A2
+    k_lincomb<<<ew, 256, 0, ctx->stream>>>(NN, wfact, C0.p, 0.5 * wfact, C1.p, C2.p);
+    GC_LAUNCHED(ctx);
+    k_lincomb<<<ew, 256, 0, ctx->stream>>>(NN, 1.0, com, 1.0, C2.p, com);
+    GC_LAUNCHED(ctx);
+    double fact = 1.0;
+    double *c0 = C0.p, *c1 = C1.p, *c2 = C2.p;
+    for (int nord = 2; nord <= max_cn; ++nord) {
+      fact *= nord;
+      GC_CUBLAS(ctx, mm(w0.p, c1, c2, one, zero));
+      GC_CUBLAS(ctx, mm(w1.p, c0, c2, -(double)nord * (nord - 1), -(double)nord));
+      k_lincomb<<<ew, 256, 0, ctx->stream>>>(NN, 1.0, com, wfact / fact / (nord + 1), c2, com);
+      GC_LAUNCHED(ctx);
+      double *t = c0;
+      c0 = c1;
+      c1 = c2;
+      c2 = t;
+    }
+  }
+  infos.resize(nfreq);
+  GC_CUDA(ctx, cudaMemcpyAsync(infos.data(), dinfo.p, nfreq * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < nfreq; ++k)
+    if (infos[k] != 0)
+      return gc::set_error(ctx, GC_ECUSOLVER, "ac_freq_fofo: A0 + omega^2 singular at point %d "
+                           "(getrf info %d)", k + 1, infos[k]);
+  return GC_OK;
+}
+
+}  // namespace
+
+namespace {
+int freq_energy(gc_context *ctx, const gc::SysDev &sd, int N, const double *com,
+                const double *fofo, int precision, double *ecorr);
 }  // namespace
 
 extern "C" int gc_freq_grid(int nfreq, double *x, double *w) {
@@ -167,8 +265,18 @@ extern "C" int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, 
   GC_TRY(gc::assemble_ab(ctx, sd, ffoo, fofo, 1.0, a1p.p, a1m.p, nullptr));
   GC_TRY(gc::axpby_into(ctx, NN, 1.0, a1p.p, -1.0, a0p.p, a1p.p));
   GC_TRY(gc::axpby_into(ctx, NN, 1.0, a1m.p, -1.0, a0m.p, a1m.p));
-  // A+0 = L L^T, L^T A-0 L = U W U^T
-  GC_TRY(gc::chol_eig(ctx, N, a0p.p, a0m.p, L.p, U.p, w.p, erpa_mode, precision));
+  // A+0 = L L^T, L^T A-0 L = U W U^T; without a Cholesky factor (A+B(0) not positive
+  // definite) the reference's LU form at every frequency
+  const int rc = gc::chol_eig(ctx, N, a0p.p, a0m.p, L.p, U.p, w.p, erpa_mode, precision);
+  if (rc == GC_ENOTPD) {
+    L.release();
+    U.release();
+    gc::DevBuf<double> com;
+    GC_TRY(com.alloc(ctx, NN));
+    GC_TRY(freq_com_lu(ctx, N, a0p.p, a0m.p, a1p.p, a1m.p, nfreq, max_cn, com.p));
+    return freq_energy(ctx, sd, N, com.p, fofo, precision, ecorr);
+  }
+  GC_TRY(rc);
   a0p.release();
   a0m.release();
   gc::DevBuf<double> B, P, K, A1t, A2t, T1;
@@ -228,13 +336,21 @@ extern "C" int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, 
   // COM = B S B^T
   GC_TRY(gemm(ctx, p, false, true, N, N, N, S.p, N, B.p, N, T1.p, N));
   GC_TRY(gemm(ctx, p, false, false, N, N, N, B.p, N, T1.p, N, T2.p, N));
+  return freq_energy(ctx, sd, N, T2.p, fofo, precision, ecorr);
+}
+
+namespace {
+
+// ECorr of WIter_FOFO from COM (ac_fofo.f90:127-181).
+int freq_energy(gc_context *ctx, const gc::SysDev &sd, int N, const double *com,
+                const double *fofo, int precision, double *ecorr) {
   const unsigned gy = (unsigned)std::min(N, 1024);
   const size_t npart = (size_t)gc::ceil_div(N, 256) * gy;
   gc::DevBuf<double> part, res;
   GC_TRY(part.alloc(ctx, npart));
   GC_TRY(res.alloc(ctx, 1));
   k_freq_energy<<<dim3(gc::ceil_div(N, 256), gy), 256, 0, ctx->stream>>>(
-      sd.n, sd.nocc, N, T2.p, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, part.p);
+      sd.n, sd.nocc, N, com, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, part.p);
   GC_LAUNCHED(ctx);
   k_sum_parts<<<1, 1024, 0, ctx->stream>>>(npart, part.p, res.p);
   GC_LAUNCHED(ctx);
@@ -245,3 +361,5 @@ extern "C" int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, 
     return gc::set_error(ctx, GC_ENONFINITE, "ac_freq_fofo: the energy is not finite");
   return GC_OK;
 }
+
+}  // namespace

@@ -271,8 +271,10 @@ int gc_freq_grid(int nfreq, double *x, double *w);
  * eigensolve of mode GC_ERPA_CHOLESKY or GC_ERPA_CHOLESKY_REFINED), so each
  * frequency costs element-wise passes and 2 (max_cn - 2) + 1 GEMMs in the given
  * precision (GC_PREC_FP64 or a sliced GC_PREC_FP64TC4/5/6) instead of an LU
- * inverse. Needs A+B(0) positive definite (GC_ENOTPD otherwise). Other arguments
- * as gc_ab_cas_fofo_ex; *etot_host = E_CAS w/o ENuc (may be NULL). */
+ * inverse. When A+B(0) is not positive definite (no Cholesky factor) the
+ * reference's own form runs instead: the LU inverse of A0 + omega^2 at every
+ * frequency (dgetrf/dgetrs) and FP64 products. Other arguments as
+ * gc_ab_cas_fofo_ex; *etot_host = E_CAS w/o ENuc (may be NULL). */
 int gc_ac_freq_fofo(gc_context *ctx, int nbas, int ninact, int nact, int ndimx,
                     const double *occ_host, const double *ure_host, const double *xone_host,
                     const int *indn_host, const double *rdm2act_host, const double *ffoo_dev,

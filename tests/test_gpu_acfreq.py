@@ -43,6 +43,21 @@ def test_acfreq_matches_oracle(gpu_lib, n, nin, nact, seed, precision, mode, tol
     assert abs(gecas - ecas) < 1e-9
 
 
+def test_acfreq_indefinite_a_plus_b_takes_the_lu_form(gpu_lib):
+    """A+B(0) not positive definite: no Cholesky factor, so the reference's LU form
+    runs at every frequency (FP64) and still matches the oracle."""
+    s = synth.make_system(n=18, nin=3, nact=4, rank=72, seed=1, eri_scale=0.25)
+    ffoo, fofo = R.transform_fofo_ffoo(s.cmo, s.ao_eri_packed(), s.nin, s.nact)
+    indn = R.pair_space(s.occ, s.nele)
+    a0p, _, _ = R.ab_cas_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo,
+                              s.rdm2act, 0.0)
+    assert np.linalg.eigvalsh(0.5 * (a0p + a0p.T)).min() < 0
+    e, _ = F.witer_fofo(s.occ, s.xone, np.eye(s.n), indn, s.nin, s.nact, ffoo, fofo, s.rdm2act)
+    ge, _ = api.ac_freq_fofo(s.occ, s.xone, indn, s.nact, s.nin, t(ffoo), t(fofo), s.rdm2act,
+                             precision="fp64tc5", erpa_mode="refined")
+    assert abs(ge - e) < 1e-9 * max(1.0, abs(e)), (ge, e)
+
+
 def test_acfreq_series_orders_and_ure(gpu_lib):
     s = synth.make_system(n=18, nin=2, nact=4, rank=72, seed=6)
     ffoo, fofo = R.transform_fofo_ffoo(s.cmo, s.ao_eri_packed(), s.nin, s.nact)
