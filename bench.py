@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--plain-energies", default=None,
                     help="file of the plain FP64 energies of this batch: read when it exists "
                          "(the check runs without the plain timing), written otherwise")
+    ap.add_argument("--tile", type=int, default=0,
+                    help="column tile of the sliced GEMMs (0: chosen per product; 64/96/128)")
     ap.add_argument("--kernel-only", type=int, default=0,
                     help="time only the tensor-core GEMM at this size (for profiling)")
     ap.add_argument("--no-cpu", action="store_true")
@@ -127,7 +129,7 @@ def whole_job_rate(world: int, nsys: int, ms: float) -> float:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the sliced
 # GEMM at the bench's roofline shape, from a one-launch ncu capture of
 # `bench.py --kernel-only N --precision P` (summarised under profiles/).
-GEMM_TRAFFIC: dict = {}
+GEMM_TRAFFIC: dict = {("fp64tc5", 6290): 5219443712 + 316723456}
 
 
 def read_peaks():
@@ -408,8 +410,10 @@ def run_ours(args):
 
     if args.kernel_only:
         n = args.kernel_only
+        api.default_context(0).set_gemm_tile(args.tile)
         ms_k = api.tc_gemm_time(n, n, n, args.precision, reps=3)
-        print(json.dumps({"kernel": f"tcgen05 GEMM {args.precision} {n}^3", "ms_per_launch": ms_k}))
+        print(json.dumps({"kernel": f"tcgen05 GEMM {args.precision} {n}^3", "tile": args.tile,
+                          "ms_per_launch": ms_k}))
         return
 
     ens = surrogate.Ensemble.load(surrogate.MODEL) if args.surrogate else None

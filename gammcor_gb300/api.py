@@ -76,6 +76,11 @@ class Context:
         shortening it injects a timeout for tests."""
         check(self.h, load().gc_set_pipeline_wait(self.h, int(ns)))
 
+    def set_gemm_tile(self, width: int):
+        """Column tile of the sliced FP64-accurate GEMMs: 0 picks per product,
+        64/96/128 forces it (capped by the slice count); results are identical."""
+        check(self.h, load().gc_set_gemm_tile(self.h, int(width)))
+
     def eig_refine_stats(self) -> dict:
         """Refined ERPA counters: solves, dsyevd fallbacks, largest block cluster."""
         s, f, m = C.c_longlong(), C.c_longlong(), C.c_int()

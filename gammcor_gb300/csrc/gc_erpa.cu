@@ -953,6 +953,14 @@ extern "C" int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns) {
   return GC_OK;
 }
 
+extern "C" int gc_set_gemm_tile(gc_context *ctx, int width) {
+  if (!ctx) return GC_EINVAL;
+  if (width != 0 && width != 64 && width != 96 && width != 128)
+    return gc::set_error(ctx, GC_EINVAL, "GEMM tile width %d not one of 0, 64, 96, 128", width);
+  ctx->oz_tile = width;
+  return GC_OK;
+}
+
 extern "C" int gc_set_eig_refinement(gc_context *ctx, int iterations) {
   if (!ctx) return GC_EINVAL;
   if (iterations < 1 || iterations > 4)

@@ -31,6 +31,7 @@ struct gc_context {
   int refine_max_cluster = 0;        // largest cluster diagonalised in a block
   int chol_blocked = 1;              // blocked Cholesky with tensor-core trailing updates
   unsigned long long wait_ns = 1000000000ull;  // limit of the tensor-core GEMMs' pipeline waits
+  int oz_tile = 0;  // column tile of the sliced GEMMs: 0 chosen per product, else 64/96/128
   cudaEvent_t eig_ev[2] = {nullptr, nullptr};  // around each cuSOLVER eigensolve
   double eig_ms = 0.0;               // device time of the cuSOLVER eigensolves (dsyevd, ssyevd)
   long long eig_calls = 0;

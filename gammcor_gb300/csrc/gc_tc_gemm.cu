@@ -145,6 +145,34 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd
       "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
 }
 
+// As mma_bf16, with a use of the A collector buffer: C = 1 reads A from shared memory
+// and keeps it in the buffer, 2 reads the buffer, 3 reads it and releases it, 0
+// discards it (the plain form). The same A descriptor is given with every use.
+template <int C>
+__device__ __forceinline__ void mma_bf16_ca(uint32_t tmem, uint64_t ad, uint64_t bd,
+                                            uint32_t idesc, uint32_t accumulate) {
+  if constexpr (C == 1)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+  else if constexpr (C == 2)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+  else if constexpr (C == 3)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate));
+  else
+    mma_bf16(tmem, ad, bd, idesc, accumulate);
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -328,7 +356,11 @@ __global__ void __launch_bounds__(192, 1)
 // The products of one weight d = t+u share a TMEM accumulator; K is cut into
 // chunks short enough that every FP32 partial sum is an integer below 2^24, so
 // each chunk is exact, and the epilogue adds the chunks in FP64 registers.
-constexpr int OZ_BN = 64;
+// Column tile (TBN rows of B): the S weight accumulators take S * TBN of the 512 TMEM
+// columns, so TBN = 128 for S = 4, 96 for S = 5 and 64 for S = 6 at most. A wider
+// tile reads fewer operand bytes per product (shared memory and L2); a narrower
+// one gives more CTAs to a small product. oz_tile() picks one per GEMM; every
+// width gives the same result bits (each element's integer sums are the same).
 constexpr int OZ_BK = 32;      // K per stage: 32 BF16 = one 64-byte swizzled row
 constexpr int OZ_STAGES = 3;   // each stage holds every slice of A and of B
 constexpr int OZ_MAXS = 6;
@@ -337,9 +369,13 @@ constexpr int OZ_MAXS = 6;
 // visible in the result (the integer slices cannot carry them).
 constexpr int kBadExp = 0x7fffffff;
 
-constexpr int OZ_EPI_WARPS = 8;                   // two per TMEM lane quarter
-constexpr int OZ_GROUP_M = 8;                     // row tiles per raster group
-constexpr int OZ_THREADS = 64 + 32 * OZ_EPI_WARPS;  // TMA warp, MMA warp, epilogue
+constexpr int OZ_GROUP_M = 8;  // row tiles per raster group
+// Epilogue: four warps (one per TMEM lane quarter) per 32 columns of the tile.
+__host__ __device__ constexpr int oz_epi_warps(int tbn) { return 4 * (tbn / 32); }
+__host__ __device__ constexpr int oz_threads(int tbn) {  // TMA warp, MMA warp, epilogue
+  return 64 + 32 * oz_epi_warps(tbn);
+}
+__host__ __device__ constexpr int oz_max_tile(int S) { return S <= 4 ? 128 : (S == 5 ? 96 : 64); }
 
 struct OzPlan {
   int S;          // slices per operand
@@ -362,17 +398,19 @@ struct OzEpi {
                          // tri_period-wide column block (C lower-triangular per block)
 };
 
-template <int S>
-__global__ void __launch_bounds__(OZ_THREADS, 1)
+template <int S, int TBN>
+__global__ void __launch_bounds__(oz_threads(TBN), 1)
     k_tc_gemm_oz(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                  int M, int N, int kblocks, int a_batched, int b_batched, OzPlan plan, OzEpi epi,
                  int *err_flag, unsigned long long wait_ns) {
   // One stage = the K block [kb*32, kb*32+32) of all S slices of the A tile (128 rows)
-  // and of the B tile (OZ_BN rows): every slice product t+u < S of the block is
+  // and of the B tile (TBN rows): every slice product t+u < S of the block is
   // issued from it, so each slice tile crosses L2 -> shared memory once per block.
+  static_assert(S * TBN <= 512 && TBN % 32 == 0, "S weight accumulators exceed TMEM");
+  constexpr int EPI = oz_epi_warps(TBN);
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr uint32_t A_BYTES = BM * OZ_BK * 2, B_BYTES = OZ_BN * OZ_BK * 2;
+  constexpr uint32_t A_BYTES = BM * OZ_BK * 2, B_BYTES = TBN * OZ_BK * 2;
   constexpr uint32_t STAGE_BYTES = S * (A_BYTES + B_BYTES);
   uint64_t *full = (uint64_t *)(smem + OZ_STAGES * STAGE_BYTES);
   uint64_t *empty = full + OZ_STAGES;
@@ -382,7 +420,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   uint32_t *tmem_slot = (uint32_t *)(drainb + 1);
   __shared__ int abort_flag;
   volatile int *abort_v = &abort_flag;
-  __shared__ double red[OZ_EPI_WARPS];
+  __shared__ double red[EPI];
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   // Grouped raster: CTAs are scheduled roughly in linear order, so consecutive ones
@@ -400,11 +438,11 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     mt = first_m + r % gm;
     nt = r / gm;
   }
-  const int m0 = mt * BM, n0 = nt * OZ_BN, b = blockIdx.z;
+  const int m0 = mt * BM, n0 = nt * TBN, b = blockIdx.z;
   const int nchunks = (kblocks + plan.chunk_kb - 1) / plan.chunk_kb;
   if (epi.tri_period > 0) {  // whole CTA, before any barrier or TMEM is set up
     const int c0 = n0 % epi.tri_period;
-    if (c0 + OZ_BN <= epi.tri_period && c0 >= m0 + BM) return;
+    if (c0 + TBN <= epi.tri_period && c0 >= m0 + BM) return;
   }
 
   if (threadIdx.x == 0) {
@@ -413,7 +451,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(accf, 1);
-    mbar_init(acce, OZ_EPI_WARPS);
+    mbar_init(acce, EPI);
     mbar_init(drainb, 1);
     abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -452,7 +490,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       for (int j = (issued > OZ_STAGES ? issued - OZ_STAGES : 0); j < issued; ++j)
         mbar_wait(&full[j % OZ_STAGES], (j / OZ_STAGES) & 1, kDrainNs);
   } else if (warp == 1 && lane == 0) {
-    constexpr uint32_t idesc = instr_desc(OZ_BN);
+    constexpr uint32_t idesc = instr_desc(TBN);
     bool ok = true;
     for (int g = 0; g < nchunks && ok; ++g) {
       if (g > 0 && !mbar_wait(acce, (g - 1) & 1, wait_ns)) {
@@ -470,17 +508,29 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t a_base = smem_u32(smem + s * STAGE_BYTES);
         const uint32_t b_base = a_base + S * A_BYTES;
+        // A slice t at K step kk meets the B slices u < S - t back to back, so it is
+        // read from shared memory once and then from the collector buffer. The first
+        // product into weight t+u in the chunk is (0, t+u) at kb0, kk 0.
 #pragma unroll
         for (int t = 0; t < S; ++t)
 #pragma unroll
-          for (int u = 0; u + t < S; ++u)
+          for (int kk = 0; kk < OZ_BK / 16; ++kk) {
+            const uint64_t ad = smem_desc64(a_base + t * A_BYTES + kk * 32);
+            const uint32_t acc_in = (kb == kb0 && t == 0 && kk == 0) ? 0u : 1u;
+            if (t == S - 1) {
+              mma_bf16_ca<0>(tmem + (uint32_t)(t * TBN), ad, smem_desc64(b_base + kk * 32), idesc,
+                             acc_in);
+              continue;
+            }
+            mma_bf16_ca<1>(tmem + (uint32_t)(t * TBN), ad, smem_desc64(b_base + kk * 32), idesc,
+                           acc_in);
 #pragma unroll
-            for (int kk = 0; kk < OZ_BK / 16; ++kk)
-              // the first product into weight t+u in the chunk is (0, t+u) at kb0, kk 0
-              mma_bf16(tmem + (uint32_t)((t + u) * OZ_BN),
-                       smem_desc64(a_base + t * A_BYTES + kk * 32),
-                       smem_desc64(b_base + u * B_BYTES + kk * 32), idesc,
-                       (kb == kb0 && t == 0 && kk == 0) ? 0u : 1u);
+            for (int u = 1; u + t < S - 1; ++u)
+              mma_bf16_ca<2>(tmem + (uint32_t)((t + u) * TBN), ad,
+                             smem_desc64(b_base + u * B_BYTES + kk * 32), idesc, acc_in);
+            mma_bf16_ca<3>(tmem + (uint32_t)((S - 1) * TBN), ad,
+                           smem_desc64(b_base + (S - 1 - t) * B_BYTES + kk * 32), idesc, acc_in);
+          }
         mma_commit(&empty[s]);
       }
       mma_commit(accf);
@@ -498,9 +548,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     // rounded to units of 2^7 first (2^-42 of the scaled product, below FP64 rounding
     // of the result). The int64 sum over chunks is converted to FP64 once, at the end:
     // the per-chunk work is integer, not FP64, arithmetic.
-    // Two warps per TMEM lane quarter (q = warp % 4), each owning half of the columns.
+    // Four warps per 32 columns (one per TMEM lane quarter, q = warp % 4); warp group
+    // h = (warp - 2) / 4 owns columns [32 h, 32 h + 32) of the tile.
     constexpr int SI = S < 5 ? S : 5;
-    constexpr int NC = OZ_BN / 2;
+    constexpr int NC = 32;
     const int q = warp & 3;
     const int h = (warp - 2) / 4;
     const int m = m0 + q * 32 + lane;
@@ -519,7 +570,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         uint32_t r[S][8];
 #pragma unroll
         for (int d = 0; d < S; ++d)
-          tmem_ld8_issue(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * OZ_BN + h * NC + c0),
+          tmem_ld8_issue(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(d * TBN + h * NC + c0),
                          r[d]);
         tmem_ld_wait();
 #pragma unroll
@@ -567,7 +618,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
   if (epi.mode == 1 && threadIdx.x == 0) {
     long long cta = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z);
     double sum = 0.0;
-    for (int w = 0; w < OZ_EPI_WARPS; ++w) sum += red[w];
+    for (int w = 0; w < EPI; ++w) sum += red[w];
     epi.partial[cta] = sum;
   }
   if (threadIdx.x == 0 && abort_flag) atomicExch(err_flag, 1);
@@ -809,7 +860,7 @@ struct OzOperand {
   gc::DevBuf<__nv_bfloat16> buf;
   gc::DevBuf<int> exps;
   CUtensorMap map;
-  int rows = 0, Kp = 0, nb = 1, S = 0;
+  int rows = 0, Kp = 0, nb = 1, S = 0, box_rows = 0;
 };
 
 bool is_oz(int precision) { return gc::is_sliced(precision); }
@@ -836,6 +887,7 @@ OzPlan oz_plan(int precision) {
 int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, int K, int nb,
                     long long sr, long long sk, long long sb, int S, int box_rows) {
   op.rows = rows;
+  op.box_rows = box_rows;
   op.Kp = (K + BK - 1) / BK * BK;
   op.nb = nb;
   op.S = S;
@@ -872,29 +924,58 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
   return GC_OK;
 }
 
-size_t oz_smem_bytes(int S) {  // alignment pad, stages, 2 * stages + 3 barriers, TMEM slot
-  return 1024 + OZ_STAGES * (size_t)S * (BM * OZ_BK * 2 + OZ_BN * OZ_BK * 2) +
+// alignment pad, stages, 2 * stages + 3 barriers, TMEM slot
+constexpr size_t oz_smem_bytes(int S, int tbn) {
+  return 1024 + OZ_STAGES * (size_t)S * (BM * OZ_BK * 2 + tbn * OZ_BK * 2) +
          (2 * OZ_STAGES + 3) * 8 + 16;
 }
+static_assert(oz_smem_bytes(4, 128) <= 232448 && oz_smem_bytes(5, 96) <= 232448 &&
+                  oz_smem_bytes(6, 64) <= 232448,
+              "sliced GEMM stages exceed the 227 KB of shared memory per CTA");
 
-template <int S>
+// Relative time per CTA of each tile width (one CTA per SM at a time), measured on
+// products large enough to fill many waves: CTA time grows less than in
+// proportion to the width because a wide tile reads fewer operand bytes per product.
+constexpr double kOzTileCost64 = 1.0, kOzTileCost96 = 1.3, kOzTileCost128 = 1.6;
+
+// Tile width for an M x N x nbatch product: the narrowest width unless a wider one
+// finishes its CTA waves (152 SMs, one CTA each) sooner by the costs above.
+int oz_tile(const gc_context *ctx, int S, long long M, long long N, long long nbatch) {
+  const int widest = oz_max_tile(S);
+  if (ctx->oz_tile > 0) return std::min(ctx->oz_tile, widest);
+  int best = 64;
+  double best_cost = 0.0;
+  for (int tbn = 64; tbn <= widest; tbn += 32) {
+    const long long ctas = (M + BM - 1) / BM * ((N + tbn - 1) / tbn) * nbatch;
+    const double cost = (double)((ctas + 151) / 152) *
+                        (tbn == 64 ? kOzTileCost64 : (tbn == 96 ? kOzTileCost96 : kOzTileCost128));
+    if (tbn == 64 || cost < best_cost) {
+      best = tbn;
+      best_cost = cost;
+    }
+  }
+  return best;
+}
+
+template <int S, int TBN>
 int launch_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N, int nbatch,
               const OzPlan &pl, const OzEpi &epi) {
   static std::once_flag once;
   static cudaError_t cfg = cudaSuccess;
   std::call_once(once, [] {
-    cfg = cudaFuncSetAttribute(k_tc_gemm_oz<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)oz_smem_bytes(S));
+    cfg = cudaFuncSetAttribute(k_tc_gemm_oz<S, TBN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)oz_smem_bytes(S, TBN));
   });
   GC_CUDA(ctx, cfg);
-  dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, OZ_BN), nbatch);
-  k_tc_gemm_oz<S><<<grid, OZ_THREADS, oz_smem_bytes(S), ctx->stream>>>(
+  dim3 grid(gc::ceil_div(M, BM), gc::ceil_div(N, TBN), nbatch);
+  k_tc_gemm_oz<S, TBN><<<grid, oz_threads(TBN), oz_smem_bytes(S, TBN), ctx->stream>>>(
       A.map, B.map, M, N, A.Kp / OZ_BK, A.nb > 1 ? 1 : 0, B.nb > 1 ? 1 : 0, pl, epi, ctx->dev_flag,
       ctx->wait_ns);
   GC_LAUNCHED(ctx);
   return GC_OK;
 }
 
+// The B operand's TMA box height is the column tile width of the launch.
 int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N, int nbatch,
            const OzPlan &pl, OzEpi epi) {
   if (A.Kp != B.Kp) return gc::set_error(ctx, GC_EINVAL, "oz_gemm: K mismatch");
@@ -902,9 +983,14 @@ int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N
   epi.eb = B.exps.p;
   epi.ea_sb = A.nb > 1 ? A.rows : 0;
   epi.eb_sb = B.nb > 1 ? B.rows : 0;
-  if (pl.S == 6) return launch_oz<6>(ctx, A, B, M, N, nbatch, pl, epi);
-  if (pl.S == 4) return launch_oz<4>(ctx, A, B, M, N, nbatch, pl, epi);
-  return launch_oz<5>(ctx, A, B, M, N, nbatch, pl, epi);
+  const int w = B.box_rows;
+  if (pl.S == 6 && w == 64) return launch_oz<6, 64>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 5 && w == 64) return launch_oz<5, 64>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 5 && w == 96) return launch_oz<5, 96>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 4 && w == 64) return launch_oz<4, 64>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 4 && w == 96) return launch_oz<4, 96>(ctx, A, B, M, N, nbatch, pl, epi);
+  if (pl.S == 4 && w == 128) return launch_oz<4, 128>(ctx, A, B, M, N, nbatch, pl, epi);
+  return gc::set_error(ctx, GC_EINVAL, "oz_gemm: no kernel for %d slices and tile %d", pl.S, w);
 }
 
 }  // namespace
@@ -932,14 +1018,15 @@ int tc_two_sided(gc_context *ctx, int precision, int n, int cnt, const double *M
     {
       OzOperand A, B;
       GC_TRY(make_oz_operand(ctx, A, M, n * cnt, n, 1, n, 1, 0, pl.S, BM));
-      GC_TRY(make_oz_operand(ctx, B, CX, nX, n, 1, n, 1, 0, pl.S, OZ_BN));
+      GC_TRY(make_oz_operand(ctx, B, CX, nX, n, 1, n, 1, 0, pl.S,
+                             oz_tile(ctx, pl.S, (long long)n * cnt, nX, 1)));
       OzEpi e{0, T1, (long long)n * cnt, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
       GC_TRY(run_oz(ctx, A, B, n * cnt, nX, 1, pl, e));
     }
     {
       OzOperand A, B;
       GC_TRY(make_oz_operand(ctx, A, T1, nX, n, cnt, (long long)n * cnt, 1, n, pl.S, BM));
-      GC_TRY(make_oz_operand(ctx, B, CY, nY, n, 1, n, 1, 0, pl.S, OZ_BN));
+      GC_TRY(make_oz_operand(ctx, B, CY, nY, n, 1, n, 1, 0, pl.S, oz_tile(ctx, pl.S, nX, nY, cnt)));
       OzEpi e{0, out, nX, ostride, nullptr, nullptr, nullptr, nullptr, 0, 0};
       GC_TRY(run_oz(ctx, A, B, nX, nY, cnt, pl, e));
     }
@@ -979,7 +1066,7 @@ int tc_gemm_nt(gc_context *ctx, int precision, int m, int n, int k, const double
     OzPlan pl = oz_plan(precision);
     OzOperand a, b;
     GC_TRY(make_oz_operand(ctx, a, A, m, k, 1, 1, lda, 0, pl.S, BM));
-    GC_TRY(make_oz_operand(ctx, b, B, n, k, 1, 1, ldb, 0, pl.S, OZ_BN));
+    GC_TRY(make_oz_operand(ctx, b, B, n, k, 1, 1, ldb, 0, pl.S, oz_tile(ctx, pl.S, m, n, 1)));
     OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
     GC_TRY(run_oz(ctx, a, b, m, n, 1, pl, e));
     return GC_OK;  // the device flag is read at the caller's next sync point
@@ -1003,7 +1090,7 @@ int tc_gemm_strided(gc_context *ctx, int precision, int M, int N, int K, const d
   OzPlan pl = oz_plan(precision);
   OzOperand a, b;
   GC_TRY(make_oz_operand(ctx, a, A, M, K, 1, sam, sak, 0, pl.S, BM));
-  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
+  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, oz_tile(ctx, pl.S, M, N, 1)));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
   return GC_OK;  // the device flag is read at the caller's next sync point
@@ -1017,7 +1104,7 @@ int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, c
   OzPlan pl = oz_plan(precision);
   OzOperand a, b;
   GC_TRY(make_oz_operand(ctx, a, A, M, K, 1, sam, sak, 0, pl.S, BM));
-  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, OZ_BN));
+  GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, oz_tile(ctx, pl.S, M, N, 1)));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, period};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
   return GC_OK;  // the device flag is read at the caller's next sync point
@@ -1029,8 +1116,8 @@ int tc_dot_gemm(gc_context *ctx, int precision, int N, const double *Ksym, const
     OzPlan pl = oz_plan(precision);
     OzOperand a, b;
     GC_TRY(make_oz_operand(ctx, a, Ksym, N, N, 1, N, 1, 0, pl.S, BM));
-    GC_TRY(make_oz_operand(ctx, b, Y, N, N, 1, N, 1, 0, pl.S, OZ_BN));
-    size_t ncta = (size_t)ceil_div(N, BM) * ceil_div(N, OZ_BN);
+    GC_TRY(make_oz_operand(ctx, b, Y, N, N, 1, N, 1, 0, pl.S, oz_tile(ctx, pl.S, N, N, 1)));
+    size_t ncta = (size_t)ceil_div(N, BM) * ceil_div(N, b.box_rows);
     DevBuf<double> part;
     GC_TRY(part.alloc(ctx, ncta));
     OzEpi e{1, nullptr, N, 0, Y, part.p, nullptr, nullptr, 0, 0};
@@ -1122,7 +1209,7 @@ extern "C" int gc_tc_gemm_time(gc_context *ctx, int precision, int m, int n, int
     OzPlan pl = oz_plan(precision);
     OzOperand A, B;
     GC_TRY(make_oz_operand(ctx, A, a.p, m, k, 1, k, 1, 0, pl.S, BM));
-    GC_TRY(make_oz_operand(ctx, B, b.p, n, k, 1, k, 1, 0, pl.S, OZ_BN));
+    GC_TRY(make_oz_operand(ctx, B, b.p, n, k, 1, k, 1, 0, pl.S, oz_tile(ctx, pl.S, m, n, 1)));
     OzEpi e{0, c.p, m, 0, nullptr, nullptr, nullptr, nullptr, 0, 0};
     GC_TRY(run_oz(ctx, A, B, m, n, 1, pl, e));  // warm-up
     GC_CUDA(ctx, cudaEventRecord(ev.a, ctx->stream));

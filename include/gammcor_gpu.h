@@ -98,6 +98,11 @@ int gc_set_chol_blocked(gc_context *ctx, int on);
  * usable. Shortening the limit is a fault-injection setting for tests; no
  * counterpart in the reference. */
 int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns);
+/* Column tile width of the FP64-accurate sliced GEMMs (GC_PREC_FP64TC4/5/6): 0
+ * (the default) picks one per product from its shape, 64, 96 or 128 forces it
+ * (capped at 128 for FP64TC4, 96 for FP64TC5, 64 for FP64TC6). Every width gives
+ * the same result bits; only the speed differs. No counterpart in the reference. */
+int gc_set_gemm_tile(gc_context *ctx, int width);
 /* Counters of GC_ERPA_CHOLESKY_REFINED on a context: solves, solves that fell back to
  * dsyevd, and the largest cluster of close eigenvalues diagonalised in a block. */
 int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,

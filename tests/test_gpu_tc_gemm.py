@@ -11,6 +11,7 @@ import pytest
 import torch
 
 from gammcor_gb300 import api
+from gammcor_gb300._lib import GcError
 
 pytestmark = pytest.mark.gpu
 BOUND = {"bf16x3": 2e-5, "bf16x6": 1e-6, "fp64tc4": 2e-8, "fp64tc5": 5e-10, "fp64tc6": 5e-12}
@@ -52,3 +53,35 @@ def test_tc_gemm_repeated_calls_agree(gpu_lib):
     c1 = api.tc_gemm_nt(A, B, "bf16x6")
     c2 = api.tc_gemm_nt(A, B, "bf16x6")
     assert torch.equal(c1, c2)
+
+
+@pytest.mark.parametrize("precision,widths", [("fp64tc4", (64, 96, 128)), ("fp64tc5", (64, 96)),
+                                              ("fp64tc6", (64,))])
+def test_sliced_gemm_tile_widths_give_identical_bits(gpu_lib, precision, widths):
+    """Every column tile width computes each element from the same exact integer
+    sums, so forced widths and the automatic choice agree bit for bit, ragged
+    edges included (n not a multiple of any width)."""
+    g = torch.Generator(device="cuda").manual_seed(11)
+    A = torch.randn(1000, 513, dtype=torch.float64, device="cuda", generator=g)
+    B = torch.randn(700, 513, dtype=torch.float64, device="cuda", generator=g)
+    A[:, ::5] *= 1e-4
+    ctx = api.Context(0)
+    try:
+        ref = api.tc_gemm_nt(A, B, precision, ctx=ctx)
+        for w in widths:
+            ctx.set_gemm_tile(w)
+            assert torch.equal(api.tc_gemm_nt(A, B, precision, ctx=ctx), ref), w
+        ctx.set_gemm_tile(0)
+    finally:
+        ctx.close()
+    exact = A @ B.T
+    assert ((ref - exact).abs() / (A.abs() @ B.abs().T)).max().item() < BOUND[precision]
+
+
+def test_gemm_tile_setting_rejects_other_widths(gpu_lib):
+    ctx = api.Context(0)
+    try:
+        with pytest.raises(GcError):
+            ctx.set_gemm_tile(80)
+    finally:
+        ctx.close()
