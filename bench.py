@@ -461,6 +461,8 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     l0 = ctx.launches()
     eig0 = ctx.eig_time()
+    ctx.set_phase_timing(True)
+    ph0 = ctx.phase_times()
     ms = ems = 0.0
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
@@ -479,10 +481,17 @@ def run_ours(args):
     ems /= args.steps
     launches = (ctx.launches() - l0) // args.steps
     eig1 = ctx.eig_time()
+    ph1 = ctx.phase_times()
+    ctx.set_phase_timing(False)
     eig = {"device_ms_per_step": (eig1[0] - eig0[0]) / args.steps,
            "calls_per_step": (eig1[1] - eig0[1]) // args.steps,
            "what": "cuSOLVER eigensolves (ssyevd of the refined form, dsyevd fallbacks), CUDA "
                    "events around each call, summed over the concurrent worker streams"}
+    phases = {k: {"device_ms_per_step": (ph1[k][0] - ph0[k][0]) / args.steps,
+                  "calls_per_step": (ph1[k][1] - ph0[k][1]) // args.steps} for k in ph1}
+    phases["what"] = ("CUDA events around each phase on its worker stream, summed over the "
+                      "concurrent workers (a phase's time includes the slowdown from the "
+                      "others running beside it)")
     ms, ems = max_over_ranks([ms, ems], world, dev)
     value = whole_job_rate(world, args.nsys, ms)
     e2e = {"value": whole_job_rate(world, args.nsys, ems), "unit": "energies/s",
@@ -573,7 +582,7 @@ def run_ours(args):
                 "data": "synthetic", "config": workload_config(args), "method": method,
                 "surrogate_fallback_rate": float(fb.mean()),
                 "erpa_solves_per_energy": float(2 + 6 * fb.mean()) if ens else float(args.ngrid),
-                "plain_fp64": plain, "eigensolve": eig,
+                "plain_fp64": plain, "eigensolve": eig, "phases": phases,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk.summary(), "failed_systems": int((status != 0).sum()),
                 "eig_refine_stats": ctx.eig_refine_stats()}

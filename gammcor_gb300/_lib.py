@@ -43,6 +43,8 @@ SIGNATURES = {
     "gc_synchronize": (C.c_int, [_vp]),
     "gc_kernel_launches": (C.c_longlong, [_vp]),
     "gc_eig_time": (C.c_int, [_vp, _dp, C.POINTER(C.c_longlong)]),
+    "gc_set_phase_timing": (C.c_int, [_vp, C.c_int]),
+    "gc_phase_time": (C.c_int, [_vp, C.c_int, _dp, C.POINTER(C.c_longlong)]),
     "gc_set_eig_emulation": (C.c_int, [_vp, C.c_int]),
     "gc_set_eig_refinement": (C.c_int, [_vp, C.c_int]),
     "gc_set_chol_blocked": (C.c_int, [_vp, C.c_int]),

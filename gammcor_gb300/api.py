@@ -55,6 +55,21 @@ class Context:
         check(self.h, load().gc_eig_time(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    PHASES = ("transform", "assembly", "cholesky", "products", "eigen", "integrand")
+
+    def set_phase_timing(self, on: bool):
+        """Record CUDA events around each phase of the AC path (gc_phase)."""
+        check(self.h, load().gc_set_phase_timing(self.h, int(on)))
+
+    def phase_times(self) -> dict:
+        """{phase: (milliseconds, calls)} accumulated on this context so far."""
+        out = {}
+        for i, name in enumerate(self.PHASES):
+            ms, n = C.c_double(), C.c_longlong()
+            check(self.h, load().gc_phase_time(self.h, i, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
     def sync(self):
         check(self.h, load().gc_synchronize(self.h))
 

@@ -17,6 +17,59 @@ __global__ void k_axpby(size_t count, double a, const double *__restrict__ x, do
 
 namespace gc {
 
+namespace {
+cudaEvent_t phase_event(gc_context *ctx) {
+  if (!ctx->phase_pool.empty()) {
+    cudaEvent_t e = ctx->phase_pool.back();
+    ctx->phase_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+}
+}  // namespace
+
+PhaseScope::PhaseScope(gc_context *ctx, int phase) : ctx_(ctx), phase_(phase) {
+  if (!ctx_ || !ctx_->phase_on) return;
+  a_ = phase_event(ctx_);
+  if (a_ && cudaEventRecord(a_, ctx_->stream) != cudaSuccess) {
+    ctx_->phase_pool.push_back(a_);
+    a_ = nullptr;
+  }
+}
+
+PhaseScope::~PhaseScope() {
+  if (!a_) return;
+  cudaEvent_t b = phase_event(ctx_);
+  if (!b || cudaEventRecord(b, ctx_->stream) != cudaSuccess) {
+    ctx_->phase_pool.push_back(a_);
+    if (b) ctx_->phase_pool.push_back(b);
+    return;
+  }
+  ctx_->phase_pending.push_back({phase_, a_, b});
+  phase_collect(ctx_, false);
+}
+
+void phase_collect(gc_context *ctx, bool wait) {
+  std::vector<gc_phase_rec> keep;
+  for (const gc_phase_rec &r : ctx->phase_pending) {
+    cudaError_t q = wait ? cudaEventSynchronize(r.b) : cudaEventQuery(r.b);
+    if (q == cudaErrorNotReady) {
+      keep.push_back(r);
+      continue;
+    }
+    float ms = 0.f;
+    if (q == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      ctx->phase_ms[r.phase] += ms;
+      ctx->phase_calls[r.phase]++;
+    }
+    ctx->phase_pool.push_back(r.a);
+    ctx->phase_pool.push_back(r.b);
+  }
+  ctx->phase_pending.swap(keep);
+}
+
+
 int axpby_into(gc_context *ctx, size_t count, double a, const double *x, double b, const double *y,
                double *out) {
   unsigned grid = std::min<unsigned>(ceil_div(count, 256), 152u * 16u);
@@ -76,6 +129,11 @@ int gc_destroy(gc_context *ctx) {
   if (ctx->dev_nonfinite) cudaFree(ctx->dev_nonfinite);
   for (cudaEvent_t e : ctx->eig_ev)
     if (e) cudaEventDestroy(e);
+  for (const gc_phase_rec &r : ctx->phase_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : ctx->phase_pool) cudaEventDestroy(e);
   delete ctx;
   return GC_OK;
 }
@@ -94,6 +152,22 @@ int gc_eig_time(const gc_context *ctx, double *ms, long long *calls) {
   if (!ctx) return GC_EINVAL;
   if (ms) *ms = ctx->eig_ms;
   if (calls) *calls = ctx->eig_calls;
+  return GC_OK;
+}
+
+int gc_set_phase_timing(gc_context *ctx, int on) {
+  if (!ctx) return GC_EINVAL;
+  ctx->phase_on = on ? 1 : 0;
+  return GC_OK;
+}
+
+int gc_phase_time(gc_context *ctx, int phase, double *ms, long long *calls) {
+  if (!ctx) return GC_EINVAL;
+  if (phase < 0 || phase >= GC_PHASE_COUNT)
+    return gc::set_error(ctx, GC_EINVAL, "phase %d outside 0..%d", phase, GC_PHASE_COUNT - 1);
+  gc::phase_collect(ctx, true);
+  if (ms) *ms = ctx->phase_ms[phase];
+  if (calls) *calls = ctx->phase_calls[phase];
   return GC_OK;
 }
 

@@ -593,6 +593,7 @@ static int build_z(gc_context *ctx, const SysDev &sd, const double *ffoo, const 
 
 int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const double *fofo,
                 double alpha, double *abplus, double *abmin, double *etot_host, int ab1) {
+  PhaseScope ph(ctx, GC_PHASE_ASSEMBLY);
   Geo g{sd.n, sd.nin, sd.nact, sd.nocc, ab1 ? 0.0 : 1.0, ab1 ? 1 : 0};
   const int n = sd.n, N = sd.ndimx;
   ZBufs Zb;

@@ -107,6 +107,7 @@ int eval_points(gc_context *ctx, const gc_system &s, const gc_ac_params &par, Sy
   for (int i = 0; i < np; ++i) {
     const double lam = x[i];
     if (par.affine) {
+      gc::PhaseScope ph(ctx, GC_PHASE_ASSEMBLY);
       GC_TRY(gc::axpby_into(ctx, NN, 1.0 - lam, st.a0p.p, lam, st.a1p.p, ap.p));
       GC_TRY(gc::axpby_into(ctx, NN, 1.0 - lam, st.a0m.p, lam, st.a1m.p, am.p));
     } else {
@@ -171,7 +172,10 @@ int run_tasks(gc_context *ctx, std::vector<Worker> &ws, int ntask,
   cudaEvent_t start;
   GC_CUDA(ctx, cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
   GC_CUDA(ctx, cudaEventRecord(start, ctx->stream));
-  for (auto &w : ws) GC_CUDA(ctx, cudaStreamWaitEvent(w.stream, start, 0));
+  for (auto &w : ws) {
+    GC_CUDA(ctx, cudaStreamWaitEvent(w.stream, start, 0));
+    w.ctx->phase_on = ctx->phase_on;
+  }
   std::atomic<int> next{0};
   std::atomic<int> first_err{GC_OK};
   std::mutex err_mu;
@@ -206,6 +210,13 @@ int run_tasks(gc_context *ctx, std::vector<Worker> &ws, int ntask,
     ctx->refine_max_cluster = std::max(ctx->refine_max_cluster, w.ctx->refine_max_cluster);
     ctx->eig_ms += w.ctx->eig_ms;
     ctx->eig_calls += w.ctx->eig_calls;
+    gc::phase_collect(w.ctx, true);
+    for (int p = 0; p < GC_PHASE_COUNT; ++p) {
+      ctx->phase_ms[p] += w.ctx->phase_ms[p];
+      ctx->phase_calls[p] += w.ctx->phase_calls[p];
+      w.ctx->phase_ms[p] = 0.0;
+      w.ctx->phase_calls[p] = 0;
+    }
     w.ctx->launches = w.ctx->refine_solves = w.ctx->refine_fallbacks = w.ctx->eig_calls = 0;
     w.ctx->eig_ms = 0.0;
   }

@@ -792,7 +792,10 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     if (bad)
       return set_error(ctx, GC_ENONFINITE, "erpa: %d non-finite elements in A+B / A-B", bad);
   }
-  if (mode == GC_ERPA_VEC) return erpavec(ctx, N, abplus, abmin, Y, eig);
+  if (mode == GC_ERPA_VEC) {
+    PhaseScope ph(ctx, GC_PHASE_EIGEN);
+    return erpavec(ctx, N, abplus, abmin, Y, eig);
+  }
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
   k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abplus);
   GC_LAUNCHED(ctx);
@@ -806,7 +809,11 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_TRY(H.alloc(ctx, NN));
     GC_CUDA(ctx, cudaMemcpyAsync(V.p, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
-    GC_TRY(syevd(ctx, N, V.p, eig));
+    {
+      PhaseScope ph(ctx, GC_PHASE_EIGEN);
+      GC_TRY(syevd(ctx, N, V.p, eig));
+    }
+    PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
     k_scale_cols_sqrt_abs<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, V.p, eig, H.p);
     GC_LAUNCHED(ctx);
     // P = (V diag(sqrt|e|)) V^T, made exactly symmetric from its upper triangle
@@ -819,7 +826,10 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
                                N, &zero, H.p, N));
     GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, &one, P.p, N, H.p, N,
                                &zero, V.p, N));
-    GC_TRY(syevd(ctx, N, V.p, eig));
+    {
+      PhaseScope phe(ctx, GC_PHASE_EIGEN);
+      GC_TRY(syevd(ctx, N, V.p, eig));
+    }
     // Y = P Z ; T = A- Y
     GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, N, N, &one, P.p, N, V.p, N,
                                &zero, Y, N));
@@ -839,40 +849,60 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_CUDA(ctx, cudaMemcpyAsync(L.p, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
     const bool tc_prec = gc::is_sliced(gemm_precision);
-    int minor = 0;
-    if (tc_prec && ctx->chol_blocked && N >= kCholBlockedMin)
-      GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, kCholBlock, &minor));
-    else
-      GC_TRY(chol_plain(ctx, N, L.p, &minor));
-    if (minor > 0)
-      return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
-    k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
-    GC_LAUNCHED(ctx);
+    {
+      PhaseScope ph(ctx, GC_PHASE_CHOLESKY);
+      int minor = 0;
+      if (tc_prec && ctx->chol_blocked && N >= kCholBlockedMin)
+        GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, kCholBlock, &minor));
+      else
+        GC_TRY(chol_plain(ctx, N, L.p, &minor));
+      if (minor > 0)
+        return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
+      k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
+      GC_LAUNCHED(ctx);
+    }
     const bool tc = gc::is_sliced(gemm_precision);
     if (tc) {
       // T = A- L (into Y as scratch); M = L^T T; after the eigensolve Y = L U.
       // Products of the FP64-accurate sliced tensor-core GEMM (L has a zero upper triangle).
-      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, abmin, 1, N, L.p, N, 1, Y, N));
-      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, N, 1, Y, N, 1, M.p, N));
-      k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
-      GC_LAUNCHED(ctx);
-      GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
-      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, 1, N, M.p, N, 1, Y, N));
-    } else {
-      // M = A- L (into Y as scratch), then M = L^T (A- L)
-      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N, Y, N));
-      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N, M.p, N));
-      if (mode == GC_ERPA_CHOLESKY_REFINED) {
+      {
+        PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+        GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, abmin, 1, N, L.p, N, 1, Y, N));
+        GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, N, 1, Y, N, 1, M.p, N));
         k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
         GC_LAUNCHED(ctx);
       }
-      GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
+      {
+        PhaseScope ph(ctx, GC_PHASE_EIGEN);
+        GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
+      }
+      PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, 1, N, M.p, N, 1, Y, N));
+    } else {
+      {
+        // M = A- L (into Y as scratch), then M = L^T (A- L)
+        PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+        GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER,
+                                   CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N,
+                                   Y, N));
+        GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER,
+                                   CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N,
+                                   M.p, N));
+        if (mode == GC_ERPA_CHOLESKY_REFINED) {
+          k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
+          GC_LAUNCHED(ctx);
+        }
+      }
+      {
+        PhaseScope ph(ctx, GC_PHASE_EIGEN);
+        GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
+      }
       // Y = L U
+      PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
       GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
                                  CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, M.p, N, Y, N));
     }
+    PhaseScope phn(ctx, GC_PHASE_PRODUCTS);
     k_norm_chol<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig);
     GC_LAUNCHED(ctx);
     k_sqrt_eig<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(N, eig);

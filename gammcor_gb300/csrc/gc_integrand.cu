@@ -91,6 +91,7 @@ namespace gc {
 
 int integrand(gc_context *ctx, const SysDev &sd, const double *Y, const double *eig,
               const double *fofo, int precision, double *w_host) {
+  PhaseScope ph(ctx, GC_PHASE_INTEGRAND);
   const int N = sd.ndimx;
   const size_t NN = (size_t)N * N;
   DevBuf<double> kt, yk, t, diag, kdiag, part;

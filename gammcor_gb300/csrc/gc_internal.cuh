@@ -15,6 +15,12 @@
 
 #include "../../include/gammcor_gpu.h"
 
+// One timed phase on a context's stream: events a (start) and b (end).
+struct gc_phase_rec {
+  int phase;
+  cudaEvent_t a, b;
+};
+
 struct gc_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -35,10 +41,33 @@ struct gc_context {
   cudaEvent_t eig_ev[2] = {nullptr, nullptr};  // around each cuSOLVER eigensolve
   double eig_ms = 0.0;               // device time of the cuSOLVER eigensolves (dsyevd, ssyevd)
   long long eig_calls = 0;
+  int phase_on = 0;                  // gc_set_phase_timing
+  double phase_ms[GC_PHASE_COUNT] = {};
+  long long phase_calls[GC_PHASE_COUNT] = {};
+  std::vector<gc_phase_rec> phase_pending;  // recorded, not yet read
+  std::vector<cudaEvent_t> phase_pool;      // timing events ready for reuse
   std::string err;
 };
 
 namespace gc {
+
+// Phase timing: a scope records an event pair around a phase on the context's
+// stream when timing is on; completed pairs are added to the phase totals
+// without waiting (phase_collect(ctx, false)) or after the stream has passed them
+// (phase_collect(ctx, true)).
+void phase_collect(gc_context *ctx, bool wait);
+class PhaseScope {
+ public:
+  PhaseScope(gc_context *ctx, int phase);
+  ~PhaseScope();
+  PhaseScope(const PhaseScope &) = delete;
+  PhaseScope &operator=(const PhaseScope &) = delete;
+
+ private:
+  gc_context *ctx_;
+  int phase_;
+  cudaEvent_t a_ = nullptr;
+};
 
 // Status propagation --------------------------------------------------------
 int set_error(gc_context *ctx, int code, const char *fmt, ...);

@@ -112,6 +112,7 @@ extern "C" int gc_tran4_gen(gc_context *ctx, int nbas, int nA, const double *CA,
                             const double *CB, int nC, const double *CC, int nD, const double *CD,
                             const double *G, double *out, int precision) {
   if (!ctx) return GC_EINVAL;
+  gc::PhaseScope ph(ctx, GC_PHASE_TRANSFORM);
   GC_TRY(check_dims(ctx, nbas, nA, nB, nC, nD));
   if (precision < GC_PREC_FP64 || precision > GC_PREC_FP64TC4)
     return gc::set_error(ctx, GC_EINVAL, "tran4_gen: unknown precision %d", precision);
@@ -149,6 +150,7 @@ extern "C" int gc_tran4_factored(gc_context *ctx, int nbas, int rank, const doub
                                  const double *CC, int nD, const double *CD, double *out,
                                  int precision) {
   if (!ctx) return GC_EINVAL;
+  gc::PhaseScope ph(ctx, GC_PHASE_TRANSFORM);
   GC_TRY(check_dims(ctx, nbas, nA, nB, nC, nD));
   if (rank <= 0) return gc::set_error(ctx, GC_EINVAL, "tran4_factored: rank=%d", rank);
   const int n = nbas;

@@ -78,6 +78,23 @@ long long gc_kernel_launches(const gc_context *ctx);
  * their number; batched calls add their workers' eigensolves. No counterpart in
  * the reference. */
 int gc_eig_time(const gc_context *ctx, double *ms, long long *calls);
+/* Phases of the AC path whose device time gc_phase_time reports. */
+enum gc_phase {
+  GC_PHASE_TRANSFORM = 0, /* FOFO and FFOO (tran4_gen / tran4_factored) */
+  GC_PHASE_ASSEMBLY = 1,  /* A+-B at a point (assembly or the affine combination) */
+  GC_PHASE_CHOLESKY = 2,  /* Cholesky factor of A+B */
+  GC_PHASE_PRODUCTS = 3,  /* the ERPA solve's products: L^T A- L, Y = L U (or A+^1/2) */
+  GC_PHASE_EIGEN = 4,     /* eigenpairs: dsyevd, or ssyevd plus the FP64 refinement */
+  GC_PHASE_INTEGRAND = 5, /* ACEneERPA */
+  GC_PHASE_COUNT = 6
+};
+/* on = 1 records CUDA events around every phase above on the context's stream
+ * (batched calls: on every worker); 0 stops recording. Totals accumulate until
+ * read. No counterpart in the reference (it reports CPU times per routine). */
+int gc_set_phase_timing(gc_context *ctx, int on);
+/* Device time of one phase so far, summed over its calls (concurrent workers'
+ * times add up), and the number of calls. Waits for the context's stream. */
+int gc_phase_time(gc_context *ctx, int phase, double *ms, long long *calls);
 /* on = 1 lets cuSOLVER run the FP64 eigensolver's internal matrix products with
  * its fixed-point FP64 emulation on tensor cores (cusolverDnSetEmulationStrategy
  * EAGER), and the FP32 eigensolver of GC_ERPA_CHOLESKY_REFINED with BF16x9

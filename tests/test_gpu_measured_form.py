@@ -60,3 +60,29 @@ def test_surrogate_gated_energy_matches_oracle(golden):
     assert st[0] == 0
     tol = 5e-9 if fb[0] else 1e-6
     assert abs(e[0] - float(d["ecorr8"])) < tol, (e[0], float(d["ecorr8"]), bool(fb[0]))
+
+
+def test_phase_timing_counts_every_phase_and_changes_no_result(golden):
+    """gc_set_phase_timing records each phase of the batched path on the workers
+    and hands the totals to the calling context; the energies are bit-identical
+    with timing on and off."""
+    d, batch = golden
+    ctx = api.Context(0)
+    try:
+        kw = dict(ngrid=4, precision="fp64tc5", erpa_mode="refined", nstreams=2, ctx=ctx)
+        e_off, _, _, st = api.ac_energy_batched(batch, **kw)
+        assert all(n == 0 for _, n in ctx.phase_times().values())
+        ctx.set_phase_timing(True)
+        e_on, _, _, st_on = api.ac_energy_batched(batch, **kw)
+        ph = ctx.phase_times()
+        ctx.set_phase_timing(False)
+    finally:
+        ctx.close()
+    assert st[0] == 0 and st_on[0] == 0
+    assert e_on[0] == e_off[0]
+    assert ph["transform"][1] == 2                # FOFO and FFOO
+    assert ph["assembly"][1] == 2 + 4             # A+-B at 0 and 1, one combination per point
+    for name in ("cholesky", "eigen", "integrand"):
+        assert ph[name][1] == 4, (name, ph[name])
+    assert ph["products"][1] >= 4
+    assert all(ms > 0.0 for ms, _ in ph.values()), ph
