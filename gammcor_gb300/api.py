@@ -83,7 +83,8 @@ class Context:
         check(self.h, load().gc_set_eig_refinement(self.h, int(iterations)))
 
     def set_chol_blocked(self, on: bool):
-        """Blocked Cholesky of A+B with tensor-core trailing updates (N >= 1536)."""
+        """This library's blocked Cholesky of A+B (64-wide FP64 blocks, tensor-core
+        trailing updates) on the sliced path; off: one cuSOLVER dpotrf."""
         check(self.h, load().gc_set_chol_blocked(self.h, int(on)))
 
     def set_pipeline_wait(self, ns: int):

@@ -162,8 +162,6 @@ int syevd(gc_context *ctx, int N, double *A, double *w) {
 // so rotations inside a cluster of (near-)equal eigenvalues do not matter; the
 // block solve only has to be exact.
 constexpr int kMaxCluster = 64;
-constexpr int kCholBlock = 256;        // blocked Cholesky: diagonal block order
-constexpr int kCholBlockedMin = 1536;  // below this order one dpotrf call is faster
 constexpr double kTau = 0.05;
 
 __global__ void k_d2f(size_t n, const double *__restrict__ a, float *__restrict__ b) {
@@ -699,60 +697,114 @@ int chol_plain(gc_context *ctx, int N, double *A, int *minor) {
   return GC_OK;
 }
 
-// A22 -= T on the lower triangle (A22 column-major with leading dimension lda,
-// T m x m with leading dimension m).
-__global__ void k_sub_lower(int m, double *__restrict__ A22, long long lda,
-                            const double *__restrict__ T) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y;
-  if (i >= m || i < j) return;
-  A22[i + (size_t)j * lda] -= T[i + (size_t)j * m];
+// Blocked Cholesky of the tensor-core path. GB300's FP64 pipe is narrow (about two
+// FP64 FMAs per cycle per SM), so the FP64 CUDA-core work is kept to what every SM
+// can share: 64-wide diagonal blocks are factored in shared memory by one CTA
+// (64^3/6 FMAs), the panel below is solved one row per thread on all SMs, and the
+// trailing update A22 -= P P^T (all but N^2 * 64 / 2 of the N^3/3 FMAs) runs on the
+// sliced FP64-accurate tensor-core GEMM, which subtracts into A22's lower triangle
+// in its epilogue.
+constexpr int kCholNb = 64;
+constexpr int kCholLd = kCholNb + 1;  // padded column stride of the shared block
+
+// Right-looking Cholesky of the kb x kb (kb <= 64) diagonal block A (leading
+// dimension lda) in shared memory; L's lower triangle is written back. A pivot that is
+// not positive (or not finite) records its global order k0 + k + 1 in *info, unless
+// an earlier block already did, and is replaced by 1 so that the rest stays finite.
+__global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict__ A, long long lda,
+                                                     int k0, int *__restrict__ info) {
+  __shared__ double s[kCholNb * kCholLd];
+  __shared__ int bad;
+  const int t = threadIdx.x;
+  for (int e = t; e < kb * kb; e += blockDim.x) {
+    const int i = e % kb, j = e / kb;
+    s[i + j * kCholLd] = i >= j ? A[i + j * lda] : 0.0;
+  }
+  if (t == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    if (t == 0) {
+      double d = s[k + k * kCholLd];
+      if (!(d > 0.0)) {
+        if (!bad) bad = k + 1;
+        d = 1.0;
+      }
+      s[k + k * kCholLd] = sqrt(d);
+    }
+    __syncthreads();
+    const double rl = 1.0 / s[k + k * kCholLd];
+    for (int i = k + 1 + t; i < kb; i += blockDim.x) s[i + k * kCholLd] *= rl;
+    __syncthreads();
+    const int w = kb - k - 1;
+    for (int e = t; e < w * w; e += blockDim.x) {
+      const int i = k + 1 + e % w, j = k + 1 + e / w;
+      if (i >= j) s[i + j * kCholLd] -= s[i + k * kCholLd] * s[j + k * kCholLd];
+    }
+    __syncthreads();
+  }
+  for (int e = t; e < kb * kb; e += blockDim.x) {
+    const int i = e % kb, j = e / kb;
+    if (i >= j) A[i + j * lda] = s[i + j * kCholLd];
+  }
+  if (t == 0 && bad && *info == 0) *info = k0 + bad;
 }
 
-// Blocked right-looking Cholesky of the lower triangle of A (N x N, column-major):
-// diagonal blocks by dpotrf (FP64), panels by dtrsm (FP64), trailing updates
-// A22 -= P P^T with the sliced tensor-core GEMM of precision prec (L L^T then
-// equals A to that product's ~2^-35 relative error). *minor = 0 on success, else
-// the order of the leading minor that is not positive definite.
-int chol_blocked(gc_context *ctx, int N, double *A, int prec, int nb, int *minor) {
+// Panel solve X L11^T = P for the m x 64 panel P below a factored 64-wide diagonal
+// block L11 (both in the matrix, leading dimension lda), X overwriting P: one thread
+// per row, forward substitution over the 64 columns in registers, L11 in shared
+// memory (row j of L at Ls[64 j ..], read as a broadcast).
+__global__ void __launch_bounds__(32) k_trsm_rows(int m, const double *__restrict__ L11,
+                                                  long long lda, double *__restrict__ P) {
+  __shared__ double Ls[kCholNb * kCholNb];
+  __shared__ double rd[kCholNb];
+  for (int e = threadIdx.x; e < kCholNb * kCholNb; e += blockDim.x) {
+    const int j = e / kCholNb, k = e % kCholNb;
+    Ls[e] = k <= j ? L11[j + k * lda] : 0.0;
+  }
+  for (int j = threadIdx.x; j < kCholNb; j += blockDim.x) rd[j] = 1.0 / L11[j + j * lda];
+  __syncthreads();
+  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  double x[kCholNb];
+#pragma unroll
+  for (int j = 0; j < kCholNb; ++j) x[j] = P[r + j * lda];
+#pragma unroll
+  for (int j = 0; j < kCholNb; ++j) {
+    double v = x[j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) v = fma(-x[k], Ls[j * kCholNb + k], v);
+    x[j] = v * rd[j];
+  }
+#pragma unroll
+  for (int j = 0; j < kCholNb; ++j) P[r + j * lda] = x[j];
+}
+
+// Cholesky A = L L^T of the lower triangle of A (N x N, column-major) in place, by the
+// kernels above and FP64-accurate products of precision prec (L L^T equals A to that
+// product's ~2^-35 relative error; the diagonal blocks and panels are FP64). The strict
+// upper triangle is left as it was. *minor = 0 on success, else the order of the first
+// leading minor that is not positive definite.
+int chol_blocked(gc_context *ctx, int N, double *A, int prec, int *minor) {
   *minor = 0;
-  const int nblk = (N + nb - 1) / nb;
-  gc::DevBuf<int> infos;
-  gc::DevBuf<double> T, work;
-  GC_TRY(infos.alloc(ctx, nblk));
-  GC_CUDA(ctx, cudaMemsetAsync(infos.p, 0, nblk * sizeof(int), ctx->stream));
-  const int m1 = N - nb;
-  if (m1 > 0) GC_TRY(T.alloc(ctx, (size_t)m1 * m1));
-  int lwork = 0;
-  GC_CUSOLVER(ctx, cusolverDnDpotrf_bufferSize(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, nb, A, N,
-                                               &lwork));
-  GC_TRY(work.alloc(ctx, std::max(lwork, 1)));
-  const double one = 1.0;
-  for (int blk = 0; blk < nblk; ++blk) {
-    const int k0 = blk * nb, kb = std::min(nb, N - k0), m = N - k0 - kb;
-    double *A11 = A + k0 + (size_t)k0 * N;
-    GC_CUSOLVER(ctx, cusolverDnDpotrf(ctx->cusolver, CUBLAS_FILL_MODE_LOWER, kb, A11, N, work.p,
-                                      lwork, infos.p + blk));
+  const long long lda = N;
+  gc::DevBuf<int> info;
+  GC_TRY(info.alloc(ctx, 1));
+  GC_CUDA(ctx, cudaMemsetAsync(info.p, 0, sizeof(int), ctx->stream));
+  for (int k0 = 0; k0 < N; k0 += kCholNb) {
+    const int kb = std::min(kCholNb, N - k0), m = N - k0 - kb;
+    double *A11 = A + k0 + (size_t)k0 * lda;
+    k_potrf_block<<<1, 256, 0, ctx->stream>>>(kb, A11, lda, k0, info.p);
+    GC_LAUNCHED(ctx);
     if (m == 0) break;
     double *P = A11 + kb;  // rows k0+kb.., columns k0..k0+kb
-    GC_CUBLAS(ctx, cublasDtrsm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
-                               CUBLAS_DIAG_NON_UNIT, m, kb, &one, A11, N, P, N));
-    GC_TRY(gc::tc_gemm_strided(ctx, prec, m, m, kb, P, 1, N, P, 1, N, T.p, m));  // T = P P^T
-    k_sub_lower<<<dim3(gc::ceil_div(m, 256), m), 256, 0, ctx->stream>>>(
-        m, A + (k0 + kb) + (size_t)(k0 + kb) * N, N, T.p);
+    k_trsm_rows<<<gc::ceil_div(m, 32), 32, 0, ctx->stream>>>(m, A11, lda, P);
     GC_LAUNCHED(ctx);
+    GC_TRY(gc::tc_syrk_sub_lower(ctx, prec, m, kb, P, 1, lda, P + (size_t)kb * lda, lda));
   }
-  std::vector<int> h(nblk);
-  GC_CUDA(ctx, cudaMemcpyAsync(h.data(), infos.p, nblk * sizeof(int), cudaMemcpyDeviceToHost,
-                               ctx->stream));
+  int h = 0;
+  GC_CUDA(ctx, cudaMemcpyAsync(&h, info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GC_TRY(gc::check_flag(ctx));  // synchronises; covers the trailing-update GEMMs
-  for (int blk = 0; blk < nblk; ++blk) {
-    if (h[blk] < 0) return gc::set_error(ctx, GC_ECUSOLVER, "potrf info=%d", h[blk]);
-    if (h[blk] > 0) {  // later blocks worked on an invalid update: report the first
-      *minor = blk * nb + h[blk];
-      break;
-    }
-  }
+  *minor = h;
   return GC_OK;
 }
 
@@ -852,8 +904,8 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     {
       PhaseScope ph(ctx, GC_PHASE_CHOLESKY);
       int minor = 0;
-      if (tc_prec && ctx->chol_blocked && N >= kCholBlockedMin)
-        GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, kCholBlock, &minor));
+      if (tc_prec && ctx->chol_blocked)
+        GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, &minor));
       else
         GC_TRY(chol_plain(ctx, N, L.p, &minor));
       if (minor > 0)
@@ -932,8 +984,8 @@ int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, 
   GC_LAUNCHED(ctx);
   const bool tc = gc::is_sliced(prec);
   int minor = 0;
-  if (tc && ctx->chol_blocked && N >= kCholBlockedMin)
-    GC_TRY(chol_blocked(ctx, N, L, prec, kCholBlock, &minor));
+  if (tc && ctx->chol_blocked)
+    GC_TRY(chol_blocked(ctx, N, L, prec, &minor));
   else
     GC_TRY(chol_plain(ctx, N, L, &minor));
   if (minor > 0)

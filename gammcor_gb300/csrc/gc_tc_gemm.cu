@@ -386,7 +386,7 @@ struct OzPlan {
 };
 
 struct OzEpi {
-  int mode;              // 0 store, 1 dot with r
+  int mode;              // 0 store, 1 dot with r, 2 subtract from the lower triangle of c
   double *c;
   long long ldn, sb;
   const double *r;
@@ -603,7 +603,9 @@ __global__ void __launch_bounds__(oz_threads(TBN), 1)
           long long o = (long long)b * epi.sb + m + (long long)n * epi.ldn;
           if (epi.mode == 0)
             epi.c[o] = cv;
-          else
+          else if (epi.mode == 2) {
+            if (m >= n) epi.c[o] -= cv;
+          } else
             dot += cv * epi.r[o];
         }
       }
@@ -861,6 +863,8 @@ struct OzOperand {
   gc::DevBuf<int> exps;
   CUtensorMap map;
   int rows = 0, Kp = 0, nb = 1, S = 0, box_rows = 0;
+  const __nv_bfloat16 *planes = nullptr;  // buf.p, or another operand's planes (alias)
+  const int *ex = nullptr;                // exps.p, or another operand's exponents
 };
 
 bool is_oz(int precision) { return gc::is_sliced(precision); }
@@ -882,6 +886,23 @@ OzPlan oz_plan(int precision) {
   if ((long long)(p.S + 2) * 4096 * c >= (1ll << 24)) c -= OZ_BK;
   p.chunk_kb = c / OZ_BK;
   return p;
+}
+
+// The 4-D TMA map [S][nb][rows][Kp] of an operand's slice planes, box OZ_BK x box_rows.
+int encode_oz_map(gc_context *ctx, OzOperand &op) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
+  cuuint64_t dims[4] = {(cuuint64_t)op.Kp, (cuuint64_t)op.rows, (cuuint64_t)op.nb,
+                        (cuuint64_t)op.S};
+  cuuint64_t strides[3] = {(cuuint64_t)op.Kp * 2, (cuuint64_t)op.rows * op.Kp * 2,
+                           (cuuint64_t)op.nb * op.rows * op.Kp * 2};
+  cuuint32_t box[4] = {(cuuint32_t)OZ_BK, (cuuint32_t)op.box_rows, 1, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = enc(&op.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)op.planes, dims, strides,
+                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GC_OK;
 }
 
 int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, int K, int nb,
@@ -910,18 +931,21 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
                                                              op.exps.p, op.buf.p);
   }
   GC_LAUNCHED(ctx);
-  EncodeTiledFn enc = encode_fn();
-  if (!enc) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
-  cuuint64_t dims[4] = {(cuuint64_t)op.Kp, (cuuint64_t)rows, (cuuint64_t)nb, (cuuint64_t)S};
-  cuuint64_t strides[3] = {(cuuint64_t)op.Kp * 2, (cuuint64_t)rows * op.Kp * 2,
-                           (cuuint64_t)nb * rows * op.Kp * 2};
-  cuuint32_t box[4] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows, 1, 1};
-  cuuint32_t estr[4] = {1, 1, 1, 1};
-  CUresult r = enc(&op.map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, op.buf.p, dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return gc::set_error(ctx, GC_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-  return GC_OK;
+  op.planes = op.buf.p;
+  op.ex = op.exps.p;
+  return encode_oz_map(ctx, op);
+}
+
+// A second view of src's slice planes with another TMA box height (src must outlive it).
+int alias_oz_operand(gc_context *ctx, const OzOperand &src, OzOperand &op, int box_rows) {
+  op.rows = src.rows;
+  op.Kp = src.Kp;
+  op.nb = src.nb;
+  op.S = src.S;
+  op.box_rows = box_rows;
+  op.planes = src.planes;
+  op.ex = src.ex;
+  return encode_oz_map(ctx, op);
 }
 
 // alignment pad, stages, 2 * stages + 3 barriers, TMEM slot
@@ -979,8 +1003,8 @@ int launch_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, in
 int run_oz(gc_context *ctx, const OzOperand &A, const OzOperand &B, int M, int N, int nbatch,
            const OzPlan &pl, OzEpi epi) {
   if (A.Kp != B.Kp) return gc::set_error(ctx, GC_EINVAL, "oz_gemm: K mismatch");
-  epi.ea = A.exps.p;
-  epi.eb = B.exps.p;
+  epi.ea = A.ex;
+  epi.eb = B.ex;
   epi.ea_sb = A.nb > 1 ? A.rows : 0;
   epi.eb_sb = B.nb > 1 ? B.rows : 0;
   const int w = B.box_rows;
@@ -1107,6 +1131,19 @@ int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, c
   GC_TRY(make_oz_operand(ctx, b, B, N, K, 1, sbn, sbk, 0, pl.S, oz_tile(ctx, pl.S, M, N, 1)));
   OzEpi e{0, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, period};
   GC_TRY(run_oz(ctx, a, b, M, N, 1, pl, e));
+  return GC_OK;  // the device flag is read at the caller's next sync point
+}
+
+int tc_syrk_sub_lower(gc_context *ctx, int precision, int M, int K, const double *P, long long sm,
+                      long long sk, double *C, long long ldc) {
+  if (!is_oz(precision))
+    return set_error(ctx, GC_EINVAL, "syrk_sub_lower: needs a sliced FP64-accurate precision");
+  OzPlan pl = oz_plan(precision);
+  OzOperand a, b;
+  GC_TRY(make_oz_operand(ctx, a, P, M, K, 1, sm, sk, 0, pl.S, BM));
+  GC_TRY(alias_oz_operand(ctx, a, b, oz_tile(ctx, pl.S, M, M, 1)));
+  OzEpi e{2, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, M};
+  GC_TRY(run_oz(ctx, a, b, M, M, 1, pl, e));
   return GC_OK;  // the device flag is read at the caller's next sync point
 }
 

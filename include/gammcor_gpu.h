@@ -104,8 +104,9 @@ int gc_set_eig_emulation(gc_context *ctx, int on);
 /* Refinement iterations of GC_ERPA_CHOLESKY_REFINED (default 2, range 1..4). */
 int gc_set_eig_refinement(gc_context *ctx, int iterations);
 /* on = 1 (default): the Cholesky of A+B in the ERPA forms with sliced tensor-core
- * products is blocked (order 256 diagonal blocks by dpotrf, panels by dtrsm,
- * trailing updates on the sliced GEMM) for N >= 1536; on = 0: one FP64 dpotrf. */
+ * products is this library's blocked factorization (FP64 64-wide diagonal blocks
+ * and row-wise panel solves on the CUDA cores, trailing updates on the sliced
+ * GEMM); on = 0: one cuSOLVER FP64 dpotrf. The FP64 path always uses dpotrf. */
 int gc_set_chol_blocked(gc_context *ctx, int on);
 /* Limit, in nanoseconds, of every pipeline wait of the tensor-core GEMM kernels
  * launched on the context (default and maximum 1 s; 0 restores the default).

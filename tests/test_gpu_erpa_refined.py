@@ -185,13 +185,14 @@ def spd(N, seed, lo=1.0, hi=1e3, negative=0):
     return 0.5 * (A + A.T)
 
 
-def test_blocked_cholesky_matches_plain_and_numpy(gpu_lib):
-    """N = 1800 is above the blocked-Cholesky threshold: A+ = L L^T with tensor-core
-    trailing updates gives the omega and sum y y^T of the single-dpotrf form and of
-    numpy. Both forms build L^T A- L from FP64TC5 products (~2^-35 of |A||B| per
-    element); with |L^T A- L| <= 50 and omega^2 >= 0.5 that moves omega by ~1e-8
-    relative, checked at 1e-6."""
-    N = 1800
+@pytest.mark.parametrize("N", [50, 64, 65, 200, 1800])
+def test_blocked_cholesky_matches_plain_and_numpy(gpu_lib, N):
+    """The library's blocked Cholesky (64-wide FP64 blocks, row-wise panel solves,
+    tensor-core trailing updates), at orders below, at and just above one block
+    and with a ragged last block, gives the omega and sum y y^T of the single-dpotrf
+    form and of numpy. Both forms build L^T A- L from FP64TC5 products (~2^-35 of
+    |A||B| per element); with |L^T A- L| <= 50 and omega^2 >= 0.5 that moves omega
+    by ~1e-8 relative, checked at 1e-6."""
     ap, am = spd(N, 1, 1.0, 10.0), spd(N, 2, 0.5, 5.0)
     res = []
     for blocked in (True, False):
@@ -206,12 +207,17 @@ def test_blocked_cholesky_matches_plain_and_numpy(gpu_lib):
     assert np.abs(res[0][1] - res[1][1]).max() < 1e-6 * np.abs(res[1][1]).max()
 
 
-@pytest.mark.parametrize("blocked", [True, False])
-def test_cholesky_reports_not_positive_definite(gpu_lib, blocked):
+def test_cholesky_reports_not_positive_definite(gpu_lib):
+    """Both Cholesky forms return GC_ENOTPD and name the same first leading minor
+    that is not positive definite."""
     N = 1700
     ap, am = spd(N, 3, negative=1), spd(N, 4)
-    ctx = api.Context(0)
-    ctx.set_chol_blocked(blocked)
-    with pytest.raises(GcError) as ei:
-        api.erpasymm1(t(ap), t(am), mode="refined", precision="fp64tc5", ctx=ctx)
-    assert ei.value.code == 5  # GC_ENOTPD
+    minors = []
+    for blocked in (True, False):
+        ctx = api.Context(0)
+        ctx.set_chol_blocked(blocked)
+        with pytest.raises(GcError) as ei:
+            api.erpasymm1(t(ap), t(am), mode="refined", precision="fp64tc5", ctx=ctx)
+        assert ei.value.code == 5  # GC_ENOTPD
+        minors.append(int(str(ei.value).split("minor")[1].strip(" )")))
+    assert minors[0] == minors[1] > 0
