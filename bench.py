@@ -129,7 +129,7 @@ def whole_job_rate(world: int, nsys: int, ms: float) -> float:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the sliced
 # GEMM at the bench's roofline shape, from a one-launch ncu capture of
 # `bench.py --kernel-only N --precision P` (summarised under profiles/).
-GEMM_TRAFFIC: dict = {("fp64tc5", 6290): 5219443712 + 316723456}
+GEMM_TRAFFIC: dict = {("fp64tc5", 6290): 4511958528 + 319232512}
 
 
 def read_peaks():
