@@ -957,10 +957,11 @@ static_assert(oz_smem_bytes(4, 128) <= 232448 && oz_smem_bytes(5, 96) <= 232448 
                   oz_smem_bytes(6, 64) <= 232448,
               "sliced GEMM stages exceed the 227 KB of shared memory per CTA");
 
-// Relative time per CTA of each tile width (one CTA per SM at a time), measured on
-// products large enough to fill many waves: CTA time grows less than in
-// proportion to the width because a wide tile reads fewer operand bytes per product.
-constexpr double kOzTileCost64 = 1.0, kOzTileCost96 = 1.3, kOzTileCost128 = 1.6;
+// Relative time per CTA of each tile width (one CTA per SM at a time), measured at
+// 6290^3 on GB300 (ms per wave of 152 CTAs: FP64TC5 0.227 at 64 and 0.240 at 96;
+// FP64TC4 0.171, 0.183 and 0.201 at 64, 96 and 128). A CTA's time is set by the
+// operand bytes it moves, so a wider tile costs little more per CTA.
+constexpr double kOzTileCost64 = 1.0, kOzTileCost96 = 1.06, kOzTileCost128 = 1.18;
 
 // Tile width for an M x N x nbatch product: the narrowest width unless a wider one
 // finishes its CTA waves (152 SMs, one CTA each) sooner by the costs above.
