@@ -261,15 +261,13 @@ __global__ void k_ac0_back_right(int N, const double *__restrict__ work, const i
   u[(size_t)r + (size_t)c * N] = v;
 }
 
-__device__ __forceinline__ double cicoef(double o) { return o >= 0.5 ? sqrt(o) : -sqrt(o); }
-
 // C[r, c] = sum_k Ybd[r, k] U[k, c] (k in the block of r), contracted on the fly with
 // (C_p + C_q)(C_r' + C_s') (r's'|pq) for pairs r = (p, q), c = (r', s') not in one orbital
 // group (the energy loop of AC0CAS_FOFO, abfofo.f90:1676-1720); one partial per CTA.
 __global__ void k_ac0_energy(int n, int nocc, int N, const double *__restrict__ u,
                              const int *__restrict__ bs, const int *__restrict__ bz,
                              const double *__restrict__ Yrow, const int *__restrict__ pp,
-                             const int *__restrict__ pq, const double *__restrict__ occ,
+                             const int *__restrict__ pq, const double *__restrict__ cpl,
                              const int *__restrict__ grp, const double *__restrict__ fofo,
                              double *__restrict__ part) {
   __shared__ double red[256];
@@ -277,7 +275,7 @@ __global__ void k_ac0_energy(int n, int nocc, int N, const double *__restrict__ 
   double e = 0.0;
   if (r < N) {
     const int p = pp[r], q = pq[r], s = bs[r], m = bz[r];
-    const double cpq = cicoef(occ[p]) + cicoef(occ[q]);
+    const double cpq = cpl[r];  // C_p + C_q
     const size_t ld = (size_t)n * nocc;
     for (int c = blockIdx.y; c < N; c += gridDim.y) {
       const int rr = pp[c], ss = pq[c];
@@ -286,7 +284,7 @@ __global__ void k_ac0_energy(int n, int nocc, int N, const double *__restrict__ 
       for (int b = 0; b < m; ++b)
         cv += Yrow[(size_t)r * kRow + b] * u[(size_t)(s + b) + (size_t)c * N];
       const double f = fofo[((size_t)rr + (size_t)ss * n) * ld + p + (size_t)q * n];  // (r's'|pq)
-      e += cpq * (cicoef(occ[rr]) + cicoef(occ[ss])) * cv * f;
+      e += cpq * cpl[c] * cv * f;
     }
   }
   red[threadIdx.x] = e;
@@ -431,7 +429,7 @@ extern "C" int gc_ac0cas_fofo(gc_context *ctx, int nbas, int ninact, int nact, i
   GC_TRY(part.alloc(ctx, npart));
   GC_TRY(res.alloc(ctx, 1));
   k_ac0_energy<<<dim3(gc::ceil_div(N, 256), gy), 256, 0, ctx->stream>>>(
-      n, nocc, N, a0p.p, pbs.p, pbz.p, Yrow.p, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo,
+      n, nocc, N, a0p.p, pbs.p, pbz.p, Yrow.p, sd.pair_p.p, sd.pair_q.p, sd.cpl.p, sd.grp.p, fofo,
       part.p);
   GC_LAUNCHED(ctx);
   k_sum<<<1, 1024, 0, ctx->stream>>>(npart, part.p, res.p);

@@ -102,27 +102,26 @@ __global__ void k_lincomb(size_t NN, double a, const double *__restrict__ x, dou
     out[e] = a * x[e] + (y ? b * y[e] : 0.0);
 }
 
-__device__ __forceinline__ double cicoef(double o) { return o >= 0.5 ? sqrt(o) : -sqrt(o); }
-
 // ECorr partials: sum over pairs i = (p, q), j = (r, s) not in one group of
 // [(C_p + C_q)(C_r + C_s) COM[i, j] - delta_ij (n_p (1 - n_q) + n_q (1 - n_p))] (rs|pq)
 // (ac_fofo.f90:127-181). One partial per CTA.
 __global__ void k_freq_energy(int n, int nocc, int N, const double *__restrict__ com,
                               const int *__restrict__ pp, const int *__restrict__ pq,
-                              const double *__restrict__ occ, const int *__restrict__ grp,
-                              const double *__restrict__ fofo, double *__restrict__ part) {
+                              const double *__restrict__ cpl, const double *__restrict__ dnq,
+                              const int *__restrict__ grp, const double *__restrict__ fofo,
+                              double *__restrict__ part) {
   __shared__ double red[256];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double e = 0.0;
   if (i < N) {
     const int p = pp[i], q = pq[i];
-    const double cpq = cicoef(occ[p]) + cicoef(occ[q]);
+    const double cpq = cpl[i];  // C_p + C_q
     const size_t ld = (size_t)n * nocc;
     for (int j = blockIdx.y; j < N; j += gridDim.y) {
       const int r = pp[j], s = pq[j];
       if (grp[p] == grp[q] && grp[q] == grp[r] && grp[r] == grp[s]) continue;
-      double a = cpq * (cicoef(occ[r]) + cicoef(occ[s])) * com[(size_t)i + (size_t)j * N];
-      if (i == j) a -= occ[p] * (1.0 - occ[q]) + occ[q] * (1.0 - occ[p]);
+      double a = cpq * cpl[j] * com[(size_t)i + (size_t)j * N];
+      if (i == j) a -= dnq[i];
       e += a * fofo[((size_t)r + (size_t)s * n) * ld + p + (size_t)q * n];  // (rs|pq)
     }
   }
@@ -350,7 +349,7 @@ int freq_energy(gc_context *ctx, const gc::SysDev &sd, int N, const double *com,
   GC_TRY(part.alloc(ctx, npart));
   GC_TRY(res.alloc(ctx, 1));
   k_freq_energy<<<dim3(gc::ceil_div(N, 256), gy), 256, 0, ctx->stream>>>(
-      sd.n, sd.nocc, N, com, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, part.p);
+      sd.n, sd.nocc, N, com, sd.pair_p.p, sd.pair_q.p, sd.cpl.p, sd.dnq.p, sd.grp.p, fofo, part.p);
   GC_LAUNCHED(ctx);
   k_sum_parts<<<1, 1024, 0, ctx->stream>>>(npart, part.p, res.p);
   GC_LAUNCHED(ctx);

@@ -299,6 +299,7 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
                      const double *__restrict__ fofo, const double *__restrict__ ffoo, Zs Z,
                      const double *__restrict__ hno, const double *__restrict__ auxi,
                      const double *__restrict__ auxio, const double *__restrict__ wmat, double lam,
+                     const double *__restrict__ rpl, const double *__restrict__ rmi,
                      double *__restrict__ abp, double *__restrict__ abm) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -410,12 +411,11 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
     v2 += (op - orr) * hno[q + (size_t)r * n] - wmat[q + (size_t)r * n] + op * aux(gp, gs, q, r);
   vp += v2;
   vm -= v2;
-  double Cp = op >= 0.5 ? sqrt(op) : -sqrt(op), Cq = oq >= 0.5 ? sqrt(oq) : -sqrt(oq);
-  double Cr = orr >= 0.5 ? sqrt(orr) : -sqrt(orr), Cs = os >= 0.5 ? sqrt(os) : -sqrt(os);
-  double d = (Cp + Cq) * (Cr + Cs);
-  if (d != 0.0) vp /= d;
-  d = (Cp - Cq) * (Cr - Cs);
-  if (d != 0.0) vm /= d;
+  // divide by (C_p + C_q)(C_r + C_s) and (C_p - C_q)(C_r - C_s) where they are not 0,
+  // as products of the pair reciprocals (no FP64 square root or division per element)
+  const double ai_ = rpl[i], aj_ = rpl[j], bi_ = rmi[i], bj_ = rmi[j];
+  if (ai_ != 0.0 && aj_ != 0.0) vp *= ai_ * aj_;
+  if (bi_ != 0.0 && bj_ != 0.0) vm *= bi_ * bj_;
   size_t o = i + (size_t)j * N;
   abp[o] = vp;
   abm[o] = vm;
@@ -516,6 +516,24 @@ int sys_upload(gc_context *ctx, SysDev &sd, int nbas, int ninact, int nact, int 
   GC_TRY(sd.grp.upload(ctx, grp.data(), n));
   GC_TRY(sd.pair_p.upload(ctx, pp.data(), ndimx));
   GC_TRY(sd.pair_q.upload(ctx, pq.data(), ndimx));
+  {
+    auto cicoef = [](double o) { return o >= 0.5 ? std::sqrt(o) : -std::sqrt(o); };
+    std::vector<double> cpl(ndimx), cmi(ndimx), rpl(ndimx), rmi(ndimx), dnq(ndimx);
+    for (int i = 0; i < ndimx; ++i) {
+      const double cp = cicoef(occ[pp[i]]), cq = cicoef(occ[pq[i]]);
+      const double op = occ[pp[i]], oq = occ[pq[i]];
+      cpl[i] = cp + cq;
+      cmi[i] = cp - cq;
+      rpl[i] = cpl[i] != 0.0 ? 1.0 / cpl[i] : 0.0;
+      rmi[i] = cmi[i] != 0.0 ? 1.0 / cmi[i] : 0.0;
+      dnq[i] = op * (1.0 - oq) + oq * (1.0 - op);
+    }
+    GC_TRY(sd.cpl.upload(ctx, cpl.data(), ndimx));
+    GC_TRY(sd.cmi.upload(ctx, cmi.data(), ndimx));
+    GC_TRY(sd.rpl.upload(ctx, rpl.data(), ndimx));
+    GC_TRY(sd.rmi.upload(ctx, rmi.data(), ndimx));
+    GC_TRY(sd.dnq.upload(ctx, dnq.data(), ndimx));
+  }
   if (xone) {
     std::vector<double> h((size_t)n * n);
     size_t t = 0;
@@ -614,7 +632,8 @@ int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const dou
        Zb.z11.p, Zb.z12.p};
   dim3 b3(32, 8), g3(ceil_div(N, 32), ceil_div(N, 8));
   k_ab<<<g3, b3, 0, ctx->stream>>>(g, N, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p, fofo, ffoo,
-                                   Z, hno.p, auxi.p, auxio.p, wmat.p, alpha, abplus, abmin);
+                                   Z, hno.p, auxi.p, auxio.p, wmat.p, alpha, sd.rpl.p, sd.rmi.p,
+                                   abplus, abmin);
   GC_LAUNCHED(ctx);
   if (ab1) {  // AB_CAS_FOFO symmetrises the AB1 matrices (sq_symmetrize, abfofo.f90:260-263)
     dim3 bs(32, 8), gs(ceil_div(N, 32), ceil_div(N, 8));

@@ -18,12 +18,14 @@ namespace {
 
 const double kSmallE = 1e-3, kBigE = 1e8;  // abfofo.f90:3808
 
-__device__ __forceinline__ double cicoef(double o) { return o >= 0.5 ? sqrt(o) : -sqrt(o); }
-
+// Kt[i, j] = mask (C_p + C_q)(C_r + C_s) (rs|pq) with the per-pair sums cpl; the
+// pair-of-pairs mask and the FOFO address are integer work, so the element costs
+// two FP64 products (GB300's FP64 pipe, not HBM, bounds this kernel otherwise).
 __global__ void k_kt(int n, int nocc, int N, const int *__restrict__ pp, const int *__restrict__ pq,
-                     const double *__restrict__ occ, const int *__restrict__ grp,
-                     const double *__restrict__ fofo, int split_diag, double *__restrict__ kt,
-                     double *__restrict__ diag, double *__restrict__ kdiag) {
+                     const double *__restrict__ cpl, const double *__restrict__ dnq,
+                     const int *__restrict__ grp, const double *__restrict__ fofo, int split_diag,
+                     double *__restrict__ kt, double *__restrict__ diag,
+                     double *__restrict__ kdiag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= N || j >= N) return;
@@ -31,12 +33,10 @@ __global__ void k_kt(int n, int nocc, int N, const int *__restrict__ pp, const i
   bool same = grp[p] == grp[q] && grp[q] == grp[r] && grp[r] == grp[s];
   size_t ld = (size_t)n * nocc;
   double f = fofo[(size_t)(r + (size_t)s * n) * ld + p + (size_t)q * n];  // (rs|pq)
-  double c = (cicoef(occ[p]) + cicoef(occ[q])) * (cicoef(occ[r]) + cicoef(occ[s]));
-  double kv = same ? 0.0 : c * f;
+  double kv = same ? 0.0 : (cpl[i] * cpl[j]) * f;
   kt[i + (size_t)j * N] = (split_diag && i == j) ? 0.0 : kv;
   if (i == j) {
-    double op = occ[p], oq = occ[q];
-    diag[i] = same ? 0.0 : -(op * (1.0 - oq) + oq * (1.0 - op)) * f;
+    diag[i] = same ? 0.0 : -dnq[i] * f;
     kdiag[i] = kv;
   }
 }
@@ -104,8 +104,8 @@ int integrand(gc_context *ctx, const SysDev &sd, const double *Y, const double *
   const int nb = 304;
   GC_TRY(part.alloc(ctx, nb));
   dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
-  k_kt<<<g2, b2, 0, ctx->stream>>>(sd.n, sd.nocc, N, sd.pair_p.p, sd.pair_q.p, sd.occ.p, sd.grp.p,
-                                   fofo, split, kt.p, diag.p, kdiag.p);
+  k_kt<<<g2, b2, 0, ctx->stream>>>(sd.n, sd.nocc, N, sd.pair_p.p, sd.pair_q.p, sd.cpl.p,
+                                   sd.dnq.p, sd.grp.p, fofo, split, kt.p, diag.p, kdiag.p);
   GC_LAUNCHED(ctx);
   k_mask_cols<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig, yk.p);
   GC_LAUNCHED(ctx);

@@ -164,6 +164,11 @@ struct SysDev {
   DevBuf<int> pair_q;      // (ndimx)
   DevBuf<double> h;        // (n, n) symmetrised one-electron MO matrix
   DevBuf<double> rv;       // RDM2val (nocc^4), RV[i + nocc*(j + nocc*(k + nocc*l))]
+  // Per pair i = (p, q), with the CI coefficients C = sign(n - 1/2) sqrt(n) of
+  // ACEneERPA_FOFO / AB_CAS_FOFO: C_p + C_q, C_p - C_q and their reciprocals (0 where
+  // the sum or difference is 0), and n_p (1 - n_q) + n_q (1 - n_p). Computed once on
+  // the host, so that the element kernels spend the narrow FP64 pipe on products only.
+  DevBuf<double> cpl, cmi, rpl, rmi, dnq;  // (ndimx)
 };
 
 // IndN (2 x N, 1-based) reordered with q outer and p inner: consecutive pairs then
