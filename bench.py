@@ -390,9 +390,16 @@ def run_ours(args):
             e1.record()
             torch.cuda.synchronize()
             torch.cuda.cudart().cudaProfilerStop()
+            ctx = api.default_context(0)
+            ctx.set_phase_timing(True)
+            ph0 = ctx.phase_times()
+            run()
+            ph1 = ctx.phase_times()
+            ctx.set_phase_timing(False)
             print(json.dumps({"acecorr_point": args.erpa, "precision": args.precision,
                               "N": len(indn), "n": s.n, "nocc": s.nocc,
-                              "ms": e0.elapsed_time(e1)}))
+                              "ms": e0.elapsed_time(e1),
+                              "phases_ms": {k: ph1[k][0] - ph0[k][0] for k in ph1}}))
             return
         abp, abm, _ = api.ab_cas_fofo(s.occ, s.xone, indn, s.nact, s.nin, ffoo, fofo, s.rdm2act, 0.5)
         api.erpasymm1(abp.clone(), abm.clone(), mode=args.erpa, precision=args.precision)  # warm-up
