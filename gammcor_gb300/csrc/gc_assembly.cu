@@ -308,109 +308,80 @@ __global__ void k_ab(Geo g, int N, const int *__restrict__ pp, const int *__rest
   int p = pp[i], q = pq[i], r = pp[j], s = pq[j];
   int gp = grp[p], gq = grp[q], gr = grp[r], gs = grp[s];
   double op = occ[p], oq = occ[q], orr = occ[r], os = occ[s];
-  double vp = 0.0, vm = 0.0, v;
-  double ac = AC(g, gp, gq, gr, gs, lam);
+  // Every term enters A+B and A-B either with the same sign (sym, accumulated in S) or
+  // with opposite signs (anti, in A); A+B = S + A, A-B = S - A (+ the Coulomb term, A-B
+  // only). Each Z term is then one FP64 FMA with its coefficient (1, 0 or lambda):
+  // GB300's FP64 pipe, not HBM, bounds this kernel.
+  double S = 0.0, A = 0.0, Mo = 0.0;
+  const double ac = AC(g, gp, gq, gr, gs, lam);
   auto ai = [](int a, int b) { return AuxInd(a, b) == 1; };
-  double X1 = (ai(gp, gr) ? op * orr : 0.0) + (ai(gq, gs) ? oq * os : 0.0) -
-              (ai(gq, gr) ? oq * orr : 0.0) - (ai(gp, gs) ? op * os : 0.0);
+  const double X1 = (ai(gp, gr) ? op * orr : 0.0) + (ai(gq, gs) ? oq * os : 0.0) -
+                    (ai(gq, gr) ? oq * orr : 0.0) - (ai(gp, gs) ? op * os : 0.0);
   if (r >= nin && p >= nin) {
+    const double t = ac * X1;
     // FOFO Coulomb: A- += 4 AC X1 (rs|pq) (its two A+ parts cancel)
-    vm += 4.0 * ac * X1 * Fofo(fofo, g, r, s, p, q);
-    // FOFO exchange: AC X1 (ps|rq), read as (rq|ps): record (r, q) is shared by a warp
-    // of consecutive p and its elements p + s n are contiguous
-    v = ac * X1 * Fofo(fofo, g, r, q, p, s);
-    vp += v;
-    vm -= v;
-    // FFOO exchange: -AC X1 (pr|qs)
-    v = -ac * X1 * Ffoo(ffoo, g, p, r, q, s);
-    vp += v;
-    vm += v;
+    Mo = 4.0 * t * Fofo(fofo, g, r, s, p, q);
+    // FOFO exchange (anti): AC X1 (ps|rq), read as (rq|ps): record (r, q) is shared by a
+    // warp of consecutive p and its elements p + s n are contiguous
+    A = t * Fofo(fofo, g, r, q, p, s);
+    // FFOO exchange (sym): -AC X1 (pr|qs)
+    S = -t * Ffoo(ffoo, g, p, r, q, s);
   }
   const bool pa = gp == 1, qa = gq == 1, ra = gr == 1, sa = gs == 1;
   const int pA = p - nin, qA = q - nin, rA = r - nin, sA = s - nin;
-  // FOFO T1 (p -> q)
-  if (p >= nin && ra && qa) {
-    v = AC(g, gp, gs, 1, 1, lam) * Z.z1[p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA))];
-    vp += v;
-    vm -= v;
-  }
-  // FOFO T3
-  if (r >= nin && sa && pa) {
-    v = AC(g, gq, gr, 1, 1, lam) * Z.z1[r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA))];
-    vp += v;
-    vm -= v;
-  }
+  // FOFO T1 (p -> q), anti
+  if (p >= nin && ra && qa)
+    A = fma(AC(g, gp, gs, 1, 1, lam),
+            Z.z1[p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA))], A);
+  // FOFO T3, anti
+  if (r >= nin && sa && pa)
+    A = fma(AC(g, gq, gr, 1, 1, lam),
+            Z.z1[r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA))], A);
   if (r >= nin && sa) {
     if (qa && p >= nin) {
-      size_t o = p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA));
-      double c = AC(g, gp, gr, 1, 1, lam);
-      v = c * Z.z4[o];  // T4
-      vp += v;
-      vm += v;
-      v = -c * Z.z7[o];  // T6 (p -> q)
-      vp += v;
-      vm -= v;
+      const size_t o = p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA));
+      const double c = AC(g, gp, gr, 1, 1, lam);
+      S = fma(c, Z.z4[o], S);   // T4
+      A = fma(-c, Z.z7[o], A);  // T6 (p -> q)
     }
     if (pa) {
-      size_t o = r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA));
-      double c = AC(g, gq, gr, 1, 1, lam);
-      v = c * Z.z5[o];  // T4 (p -> q)
-      vp += v;
-      vm -= v;
-      v = -c * Z.z6[o];  // T6
-      vp += v;
-      vm += v;
+      const size_t o = r + (size_t)n * (q + (size_t)nocc * (pA + (size_t)na * sA));
+      const double c = AC(g, gq, gr, 1, 1, lam);
+      A = fma(c, Z.z5[o], A);   // T4 (p -> q)
+      S = fma(-c, Z.z6[o], S);  // T6
     }
   }
   if (ra && pa) {
-    size_t o = q + (size_t)nocc * (s + (size_t)nocc * (pA + (size_t)na * rA));
-    double c = AC(g, gq, gs, 1, 1, lam);
-    v = c * Z.z8[o];  // FFOO T1
-    vp += v;
-    vm += v;
-    v = c * Z.z10[o];  // T2
-    vp += v;
-    vm += v;
-    v = -c * Z.z13[o];  // T5 (p -> q)
-    vp += v;
-    vm -= v;
+    const size_t o = q + (size_t)nocc * (s + (size_t)nocc * (pA + (size_t)na * rA));
+    const double c = AC(g, gq, gs, 1, 1, lam);
+    S = fma(c, Z.z8[o] + Z.z10[o], S);  // FFOO T1 + T2
+    A = fma(-c, Z.z13[o], A);           // T5 (p -> q)
   }
-  if (sa && r >= nin && qa && p >= nin) {  // FFOO T3
-    v = AC(g, gp, gr, 1, 1, lam) * Z.z9[p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA))];
-    vp += v;
-    vm += v;
-  }
+  if (sa && r >= nin && qa && p >= nin)  // FFOO T3, sym
+    S = fma(AC(g, gp, gr, 1, 1, lam),
+            Z.z9[p + (size_t)n * (r + (size_t)n * (qA + (size_t)na * sA))], S);
   if (ra && qa && p >= nin) {
-    size_t o = p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA));
-    double c = AC(g, gp, gs, 1, 1, lam);
-    v = c * Z.z11[o];  // T2 (p -> q)
-    vp += v;
-    vm -= v;
-    v = -c * Z.z12[o];  // T5
-    vp += v;
-    vm += v;
+    const size_t o = p + (size_t)n * (s + (size_t)nocc * (qA + (size_t)na * rA));
+    const double c = AC(g, gp, gs, 1, 1, lam);
+    A = fma(c, Z.z11[o], A);   // T2 (p -> q)
+    S = fma(-c, Z.z12[o], S);  // T5
   }
-  // one-body part (final loop of AB_CAS_FOFO)
+  // one-body part (final loop of AB_CAS_FOFO): sym (p = r, q = s) and anti (q = r, p = s)
   auto aux = [&](int ga, int gb, int x, int y) -> double {
     int a = AuxInd(ga, gb);
     if (a == 1) return auxi[x + (size_t)y * n];
     if (a == 2) return auxio[x + (size_t)y * n];
     return 0.0;
   };
-  double v1 = 0.0;
   if (p == r)
-    v1 += (op - os) * hno[q + (size_t)s * n] - wmat[q + (size_t)s * n] + op * aux(gp, gr, q, s);
+    S += (op - os) * hno[q + (size_t)s * n] - wmat[q + (size_t)s * n] + op * aux(gp, gr, q, s);
   if (q == s)
-    v1 += (oq - orr) * hno[p + (size_t)r * n] - wmat[p + (size_t)r * n] + oq * aux(gq, gs, p, r);
-  vp += v1;
-  vm += v1;
-  double v2 = 0.0;
+    S += (oq - orr) * hno[p + (size_t)r * n] - wmat[p + (size_t)r * n] + oq * aux(gq, gs, p, r);
   if (q == r)
-    v2 += (oq - os) * hno[p + (size_t)s * n] - wmat[p + (size_t)s * n] + oq * aux(gq, gr, p, s);
+    A += (oq - os) * hno[p + (size_t)s * n] - wmat[p + (size_t)s * n] + oq * aux(gq, gr, p, s);
   if (p == s)
-    v2 += (op - orr) * hno[q + (size_t)r * n] - wmat[q + (size_t)r * n] + op * aux(gp, gs, q, r);
-  vp += v2;
-  vm -= v2;
+    A += (op - orr) * hno[q + (size_t)r * n] - wmat[q + (size_t)r * n] + op * aux(gp, gs, q, r);
+  double vp = S + A, vm = S - A + Mo;
   // divide by (C_p + C_q)(C_r + C_s) and (C_p - C_q)(C_r - C_s) where they are not 0,
   // as products of the pair reciprocals (no FP64 square root or division per element)
   const double ai_ = rpl[i], aj_ = rpl[j], bi_ = rmi[i], bj_ = rmi[j];
