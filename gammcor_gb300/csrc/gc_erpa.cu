@@ -51,10 +51,13 @@ __global__ void k_zero_upper(int N, double *__restrict__ a) {
 // out(:, k) = V(:, k) * sqrt(|e_k|)
 __global__ void k_scale_cols_sqrt_abs(int N, const double *__restrict__ V,
                                       const double *__restrict__ e, double *__restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = blockIdx.y;
+  __shared__ double sc;  // the column's factor, once per block
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.y;
+  if (threadIdx.x == 0) sc = sqrt(fabs(e[k]));
+  __syncthreads();
   if (i >= N) return;
-  out[i + (size_t)k * N] = V[i + (size_t)k * N] * sqrt(fabs(e[k]));
+  out[i + (size_t)k * N] = V[i + (size_t)k * N] * sc;
 }
 
 // ERPASYMM1 normalisation: for omega^2 > Small, omega = sqrt, s = 2/omega y^T (A- y),
@@ -84,12 +87,16 @@ __global__ void k_norm_symm1(int N, double *__restrict__ Y, const double *__rest
 
 // Cholesky form: y_nu = L u_nu / sqrt(2 omega) for omega^2 > Small.
 __global__ void k_norm_chol(int N, double *__restrict__ Y, double *__restrict__ eig) {
-  int nu = blockIdx.y;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double w2 = eig[nu];
+  // the column's factor is formed once per block (two FP64 square roots and a division
+  // are many instructions of GB300's narrow FP64 pipe)
+  __shared__ double sc;
+  const int nu = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double w2 = eig[nu];
   if (!(w2 > kSmall)) return;
-  double om = sqrt(w2);
-  if (i < N) Y[(size_t)nu * N + i] *= 1.0 / sqrt(2.0 * om);
+  if (threadIdx.x == 0) sc = 1.0 / sqrt(2.0 * sqrt(w2));
+  __syncthreads();
+  if (i < N) Y[(size_t)nu * N + i] *= sc;
 }
 
 // *count += number of non-finite elements of a and b (n elements each).
