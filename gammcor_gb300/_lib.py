@@ -50,6 +50,7 @@ SIGNATURES = {
     "gc_set_chol_blocked": (C.c_int, [_vp, C.c_int]),
     "gc_set_pipeline_wait": (C.c_int, [_vp, C.c_ulonglong]),
     "gc_set_gemm_tile": (C.c_int, [_vp, C.c_int]),
+    "gc_set_eig_batch": (C.c_int, [_vp, C.c_int]),
     "gc_eig_refine_stats": (C.c_int, [_vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                                       C.POINTER(C.c_int)]),
     "gc_gauleg": (C.c_int, [C.c_double, C.c_double, _dp, _dp, C.c_int]),

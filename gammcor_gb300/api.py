@@ -92,6 +92,10 @@ class Context:
         shortening it injects a timeout for tests."""
         check(self.h, load().gc_set_pipeline_wait(self.h, int(ns)))
 
+    def set_eig_batch(self, on: bool):
+        """Batch the FP32 eigensolves of all lambda points of a system (batched calls)."""
+        check(self.h, load().gc_set_eig_batch(self.h, int(on)))
+
     def set_gemm_tile(self, width: int):
         """Column tile of the sliced FP64-accurate GEMMs: 0 picks per product,
         64/96/128 forces it (capped by the slice count); results are identical."""

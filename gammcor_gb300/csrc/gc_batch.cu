@@ -98,6 +98,38 @@ int eval_points(gc_context *ctx, const gc_system &s, const gc_ac_params &par, Sy
                 double *acc) {
   const int N = s.ndimx;
   const size_t NN = (size_t)N * N;
+  if (par.erpa_mode == GC_ERPA_CHOLESKY_REFINED && gc::is_sliced(par.precision) && np >= 2 &&
+      ctx->eig_batch) {
+    // all points' FP32 eigensolves in one batched call
+    double sum = 0.0;
+    auto fill = [&](int i, double *ap, double *am) -> int {
+      const double lam = x[i];
+      if (par.affine) {
+        gc::PhaseScope ph(ctx, GC_PHASE_ASSEMBLY);
+        GC_TRY(gc::axpby_into(ctx, NN, 1.0 - lam, st.a0p.p, lam, st.a1p.p, ap));
+        GC_TRY(gc::axpby_into(ctx, NN, 1.0 - lam, st.a0m.p, lam, st.a1m.p, am));
+        return GC_OK;
+      }
+      return gc::assemble_ab(ctx, st.sd, st.ffoo.p, st.fofo.p, lam, ap, am, &st.e0);
+    };
+    auto use = [&](int i, const double *Y, double *eig) -> int {
+      double wi = 0.0;
+      GC_TRY(gc::integrand(ctx, st.sd, Y, eig, st.fofo.p, par.precision, &wi));
+      if (w_out) w_out[i] = wi;
+      if (stats_out) {
+        std::vector<double> he(N);
+        GC_CUDA(ctx, cudaMemcpyAsync(he.data(), eig, N * sizeof(double), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        omega_stats(he, stats_out + (size_t)i * GC_OMEGA_STATS);
+      }
+      if (wt) sum += wt[i] * wi;
+      return GC_OK;
+    };
+    GC_TRY(gc::erpa_solve_points(ctx, N, np, par.precision, fill, use));
+    if (acc) *acc = sum;
+    return GC_OK;
+  }
   gc::DevBuf<double> ap, am, Y, eig;
   GC_TRY(ap.alloc(ctx, NN));
   GC_TRY(am.alloc(ctx, NN));
@@ -175,6 +207,7 @@ int run_tasks(gc_context *ctx, std::vector<Worker> &ws, int ntask,
   for (auto &w : ws) {
     GC_CUDA(ctx, cudaStreamWaitEvent(w.stream, start, 0));
     w.ctx->phase_on = ctx->phase_on;
+    w.ctx->eig_batch = ctx->eig_batch;
   }
   std::atomic<int> next{0};
   std::atomic<int> first_err{GC_OK};

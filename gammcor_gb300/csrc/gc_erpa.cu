@@ -8,6 +8,8 @@
 // L^T A- L is similar to A+^1/2 A- A+^1/2 (same omega^2), and Y = L u / sqrt(2 omega)
 // satisfies the same eigen-equation and normalisation, so W(lambda), which depends
 // on Y only through Y Y^T over kept modes, is unchanged. One eigensolve instead of two.
+#include <functional>
+
 #include "gc_internal.cuh"
 #include "gc_tc_gemm.cuh"
 
@@ -553,32 +555,16 @@ int product(gc_context *ctx, int prec, bool transA, int m, int n, int k, const d
 // Xout (N x N) holds the eigenvectors, lam (N) the eigenvalues (the second-order
 // Rayleigh quotients of the updated vectors), *fallback = false.
 // *fallback = true when the FP32 solver failed or a cluster could not be handled.
+int refine_from_fp32(gc_context *ctx, int N, int prec, const double *M, const float *m32,
+                     double *Xout, double *lam, bool *fallback);
+
 int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout, double *lam,
                 bool *fallback) {
   *fallback = false;
   const size_t NN = (size_t)N * N;
   gc::DevBuf<float> m32, w32, work;
-  gc::DevBuf<double> U0, U1, vbuf, dS, dG;
-  gc::DevBuf<int> cst, csz, flag;
-  gc::DevBuf<double> colm;
   GC_TRY(m32.alloc(ctx, NN));
   GC_TRY(w32.alloc(ctx, N));
-  GC_TRY(U0.alloc(ctx, 2 * NN));
-  GC_TRY(U1.alloc(ctx, 2 * NN));
-  GC_TRY(vbuf.alloc(ctx, (size_t)N * kMaxCluster));
-  GC_TRY(dS.alloc(ctx, N));
-  GC_TRY(dG.alloc(ctx, N));
-  GC_TRY(cst.alloc(ctx, N));
-  GC_TRY(csz.alloc(ctx, N));
-  GC_TRY(flag.alloc(ctx, 2));
-  GC_TRY(colm.alloc(ctx, N));
-  GC_CUDA(ctx, cudaFuncSetAttribute(k_cluster_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kClusterSmem));
-  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_right, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kBlkSmem));
-  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_left, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kBlkSmem));
-  GC_CUDA(ctx, cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), ctx->stream));
   const unsigned ew = std::min<size_t>(gc::ceil_div(NN, 256), 152 * 16);
   k_d2f<<<ew, 256, 0, ctx->stream>>>(NN, M, m32.p);
   GC_LAUNCHED(ctx);
@@ -608,9 +594,38 @@ int refined_eig(gc_context *ctx, int N, int prec, const double *M, double *Xout,
       return GC_OK;
     }
   }
-  k_f2d<<<ew, 256, 0, ctx->stream>>>(NN, m32.p, U0.p);
+  w32.release();
+  return refine_from_fp32(ctx, N, prec, M, m32.p, Xout, lam, fallback);
+}
+
+// The refinement of an FP32 start: m32 holds FP32 eigenvectors of M (column-major,
+// eigenvalues ascending). Same outputs as refined_eig.
+int refine_from_fp32(gc_context *ctx, int N, int prec, const double *M, const float *m32,
+                     double *Xout, double *lam, bool *fallback) {
+  *fallback = false;
+  const size_t NN = (size_t)N * N;
+  gc::DevBuf<double> U0, U1, vbuf, dS, dG;
+  gc::DevBuf<int> cst, csz, flag;
+  gc::DevBuf<double> colm;
+  GC_TRY(U0.alloc(ctx, 2 * NN));
+  GC_TRY(U1.alloc(ctx, 2 * NN));
+  GC_TRY(vbuf.alloc(ctx, (size_t)N * kMaxCluster));
+  GC_TRY(dS.alloc(ctx, N));
+  GC_TRY(dG.alloc(ctx, N));
+  GC_TRY(cst.alloc(ctx, N));
+  GC_TRY(csz.alloc(ctx, N));
+  GC_TRY(flag.alloc(ctx, 2));
+  GC_TRY(colm.alloc(ctx, N));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_cluster_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kClusterSmem));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_right, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kBlkSmem));
+  GC_CUDA(ctx, cudaFuncSetAttribute(k_blk_left, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)kBlkSmem));
+  GC_CUDA(ctx, cudaMemsetAsync(flag.p, 0, 2 * sizeof(int), ctx->stream));
+  const unsigned ew = std::min<size_t>(gc::ceil_div(NN, 256), 152 * 16);
+  k_f2d<<<ew, 256, 0, ctx->stream>>>(NN, m32, U0.p);
   GC_LAUNCHED(ctx);
-  m32.release();
   double *cur = U0.p, *nxt = U1.p;
   const int iters = std::max(1, std::min(4, ctx->eig_refine));
   const unsigned gN = gc::ceil_div(N, 256);
@@ -829,17 +844,183 @@ int eigen(gc_context *ctx, int N, double *M, double *w, int mode, int prec) {
   return GC_OK;
 }
 
+// bad[k] = 1 when the FP32 eigenvalues of matrix k are not finite and ascending (the
+// refinement's cluster rule pairs neighbouring columns).
+__global__ void k_ascending(int N, int np, const float *__restrict__ w, int *__restrict__ bad) {
+  const int k = blockIdx.y;
+  const float *wk = w + (size_t)k * N;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    if (!isfinite(wk[i]) || (i + 1 < N && !(wk[i] <= wk[i + 1]))) bad[k] = 1;
+}
+
+// Eigenpairs of np symmetric N x N matrices M[k] in place (vectors overwrite M[k], values
+// in w[k]) in the refined form: one batched FP32 eigensolve (cusolverDnXsyevBatched) for
+// all of them, then the refinement of each. Concurrent FP32 eigensolves of one order
+// overlap poorly on separate streams; the batched solver runs them 2-4x faster. A
+// matrix whose FP32 solve failed, or whose refinement cannot proceed, is solved alone
+// (ssyevd start, then dsyevd), as eigen() does.
+int eigen_refined_batch(gc_context *ctx, int N, int np, double *const *M, double *const *w,
+                        int prec) {
+  if (np == 1 || N > 65535) {
+    for (int k = 0; k < np; ++k) GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
+    return GC_OK;
+  }
+  const size_t NN = (size_t)N * N;
+  gc::DevBuf<float> m32, w32;
+  gc::DevBuf<int> info;
+  GC_TRY(m32.alloc(ctx, NN * np));
+  GC_TRY(w32.alloc(ctx, (size_t)N * np));
+  GC_TRY(info.alloc(ctx, 2 * (size_t)np));  // solver status, then the ascending check
+  const unsigned ew = std::min<size_t>(gc::ceil_div(NN, 256), 152 * 16);
+  for (int k = 0; k < np; ++k) {
+    k_d2f<<<ew, 256, 0, ctx->stream>>>(NN, M[k], m32.p + k * NN);
+    GC_LAUNCHED(ctx);
+  }
+  GC_CUDA(ctx, cudaMemsetAsync(info.p, 0, 2 * (size_t)np * sizeof(int), ctx->stream));
+  {
+    cusolverDnParams_t params = nullptr;
+    GC_CUSOLVER(ctx, cusolverDnCreateParams(&params));
+    struct ParamsGuard {
+      cusolverDnParams_t p;
+      ~ParamsGuard() { cusolverDnDestroyParams(p); }
+    } guard{params};
+    size_t wd = 0, wh = 0;
+    GC_CUSOLVER(ctx, cusolverDnXsyevBatched_bufferSize(
+                         ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N,
+                         CUDA_R_32F, m32.p, N, CUDA_R_32F, w32.p, CUDA_R_32F, &wd, &wh, np));
+    gc::DevBuf<char> work;
+    GC_TRY(work.alloc(ctx, std::max<size_t>(wd, 1)));
+    std::vector<char> hwork(std::max<size_t>(wh, 1));
+    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[0], ctx->stream));
+    GC_CUSOLVER(ctx, cusolverDnXsyevBatched(ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR,
+                                            CUBLAS_FILL_MODE_LOWER, N, CUDA_R_32F, m32.p, N,
+                                            CUDA_R_32F, w32.p, CUDA_R_32F, work.p, wd,
+                                            hwork.data(), wh, info.p, np));
+    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[1], ctx->stream));
+    k_ascending<<<dim3(gc::ceil_div(N, 256), np), 256, 0, ctx->stream>>>(N, np, w32.p,
+                                                                         info.p + np);
+    GC_LAUNCHED(ctx);
+    std::vector<int> h(2 * (size_t)np);
+    GC_CUDA(ctx, cudaMemcpyAsync(h.data(), info.p, 2 * (size_t)np * sizeof(int),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    GC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->eig_ev[0], ctx->eig_ev[1]));
+    ctx->eig_ms += ms;
+    ctx->eig_calls += np;
+    w32.release();
+    for (int k = 0; k < np; ++k) {
+      if (h[k] != 0 || h[np + k] != 0) {  // solved alone: the ssyevd start, then dsyevd
+        GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
+        continue;
+      }
+      ctx->refine_solves++;
+      bool fallback = false;
+      GC_TRY(refine_from_fp32(ctx, N, prec, M[k], m32.p + k * NN, M[k], w[k], &fallback));
+      if (fallback) {
+        ctx->refine_fallbacks++;
+        GC_TRY(syevd(ctx, N, M[k], w[k]));
+      }
+    }
+  }
+  return GC_OK;
+}
+
 }  // namespace
 
 namespace gc {
+
+// Checks A+-B for non-finite elements and symmetrises both in place.
+int erpa_prepare(gc_context *ctx, int N, double *abplus, double *abmin) {
+  const size_t NN = (size_t)N * N;
+  // No eigensolver is handed a matrix with a NaN or an infinity.
+  GC_CUDA(ctx, cudaMemsetAsync(ctx->dev_nonfinite, 0, sizeof(int), ctx->stream));
+  const unsigned grid = std::min<size_t>(ceil_div(NN, 256), 152 * 8);
+  k_count_nonfinite<<<grid, 256, 0, ctx->stream>>>(NN, abplus, abmin, ctx->dev_nonfinite);
+  GC_LAUNCHED(ctx);
+  int bad = 0;
+  GC_CUDA(ctx, cudaMemcpyAsync(&bad, ctx->dev_nonfinite, sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (bad) return set_error(ctx, GC_ENONFINITE, "erpa: %d non-finite elements in A+B / A-B", bad);
+  dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
+  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abplus);
+  GC_LAUNCHED(ctx);
+  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abmin);
+  GC_LAUNCHED(ctx);
+  return GC_OK;
+}
+
+// Cholesky form, first half: A+B = L L^T (L lower, zero upper triangle) and the
+// symmetric M = L^T (A-B) L, from the symmetrised A+-B. T (N x N) is scratch.
+int chol_form(gc_context *ctx, int N, const double *abplus, const double *abmin, double *L,
+              double *M, double *T, int mode, int prec) {
+  const size_t NN = (size_t)N * N;
+  const dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
+  const double one = 1.0;
+  GC_CUDA(ctx, cudaMemcpyAsync(L, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  const bool tc = gc::is_sliced(prec);
+  {
+    PhaseScope ph(ctx, GC_PHASE_CHOLESKY);
+    int minor = 0;
+    if (tc && ctx->chol_blocked)
+      GC_TRY(chol_blocked(ctx, N, L, prec, &minor));
+    else
+      GC_TRY(chol_plain(ctx, N, L, &minor));
+    if (minor > 0)
+      return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
+    k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L);
+    GC_LAUNCHED(ctx);
+  }
+  PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+  if (tc) {
+    // T = A- L; M = L^T T: products of the FP64-accurate sliced tensor-core GEMM (L has a
+    // zero upper triangle)
+    GC_TRY(tc_gemm_strided(ctx, prec, N, N, N, abmin, 1, N, L, N, 1, T, N));
+    GC_TRY(tc_gemm_strided(ctx, prec, N, N, N, L, N, 1, T, N, 1, M, N));
+    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M);
+    GC_LAUNCHED(ctx);
+  } else {
+    // T = A- L, then M = L^T T
+    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L, N, abmin, N, T, N));
+    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T,
+                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L, N, T, N, M, N));
+    if (mode == GC_ERPA_CHOLESKY_REFINED) {
+      k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M);
+      GC_LAUNCHED(ctx);
+    }
+  }
+  return GC_OK;
+}
+
+// Cholesky form, second half: Y = L U for the eigenvectors U of M (eigenvalues omega^2
+// in eig), normalised as ERPASYMM1 normalises, and eig <- omega.
+int chol_finish(gc_context *ctx, int N, const double *L, const double *U, double *Y, double *eig,
+                int prec) {
+  PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+  if (gc::is_sliced(prec)) {
+    GC_TRY(tc_gemm_strided(ctx, prec, N, N, N, L, 1, N, U, N, 1, Y, N));
+  } else {
+    const double one = 1.0;
+    GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
+                               CUBLAS_DIAG_NON_UNIT, N, N, &one, L, N, U, N, Y, N));
+  }
+  k_norm_chol<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig);
+  GC_LAUNCHED(ctx);
+  k_sqrt_eig<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(N, eig);
+  GC_LAUNCHED(ctx);
+  return GC_OK;
+}
 
 int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig,
                int mode, int gemm_precision, bool aplsqrt_out) {
   if (N <= 0 || !abplus || !abmin || !Y || !eig)
     return set_error(ctx, GC_EINVAL, "erpa: bad arguments N=%d", N);
   const size_t NN = (size_t)N * N;
-  {
-    // No eigensolver is handed a matrix with a NaN or an infinity.
+  if (mode == GC_ERPA_VEC) {
+    // ERPAVEC reads A+-B as given (the non-finite check still applies)
     GC_CUDA(ctx, cudaMemsetAsync(ctx->dev_nonfinite, 0, sizeof(int), ctx->stream));
     const unsigned grid = std::min<size_t>(ceil_div(NN, 256), 152 * 8);
     k_count_nonfinite<<<grid, 256, 0, ctx->stream>>>(NN, abplus, abmin, ctx->dev_nonfinite);
@@ -850,16 +1031,11 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (bad)
       return set_error(ctx, GC_ENONFINITE, "erpa: %d non-finite elements in A+B / A-B", bad);
-  }
-  if (mode == GC_ERPA_VEC) {
     PhaseScope ph(ctx, GC_PHASE_EIGEN);
     return erpavec(ctx, N, abplus, abmin, Y, eig);
   }
-  dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
-  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abplus);
-  GC_LAUNCHED(ctx);
-  k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, abmin);
-  GC_LAUNCHED(ctx);
+  GC_TRY(erpa_prepare(ctx, N, abplus, abmin));
+  const dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
   const double one = 1.0, zero = 0.0;
   if (mode == GC_ERPA_SYMM1) {
     DevBuf<double> V, P, H;
@@ -905,70 +1081,47 @@ int erpa_solve(gc_context *ctx, int N, double *abplus, double *abmin, double *Y,
     DevBuf<double> L, M;
     GC_TRY(L.alloc(ctx, NN));
     GC_TRY(M.alloc(ctx, NN));
-    GC_CUDA(ctx, cudaMemcpyAsync(L.p, abplus, NN * sizeof(double), cudaMemcpyDeviceToDevice,
-                                 ctx->stream));
-    const bool tc_prec = gc::is_sliced(gemm_precision);
+    GC_TRY(chol_form(ctx, N, abplus, abmin, L.p, M.p, Y, mode, gemm_precision));
     {
-      PhaseScope ph(ctx, GC_PHASE_CHOLESKY);
-      int minor = 0;
-      if (tc_prec && ctx->chol_blocked)
-        GC_TRY(chol_blocked(ctx, N, L.p, gemm_precision, &minor));
-      else
-        GC_TRY(chol_plain(ctx, N, L.p, &minor));
-      if (minor > 0)
-        return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)", minor);
-      k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, L.p);
-      GC_LAUNCHED(ctx);
+      PhaseScope ph(ctx, GC_PHASE_EIGEN);
+      GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
     }
-    const bool tc = gc::is_sliced(gemm_precision);
-    if (tc) {
-      // T = A- L (into Y as scratch); M = L^T T; after the eigensolve Y = L U.
-      // Products of the FP64-accurate sliced tensor-core GEMM (L has a zero upper triangle).
-      {
-        PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
-        GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, abmin, 1, N, L.p, N, 1, Y, N));
-        GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, N, 1, Y, N, 1, M.p, N));
-        k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
-        GC_LAUNCHED(ctx);
-      }
-      {
-        PhaseScope ph(ctx, GC_PHASE_EIGEN);
-        GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
-      }
-      PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
-      GC_TRY(tc_gemm_strided(ctx, gemm_precision, N, N, N, L.p, 1, N, M.p, N, 1, Y, N));
-    } else {
-      {
-        // M = A- L (into Y as scratch), then M = L^T (A- L)
-        PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
-        GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER,
-                                   CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, abmin, N,
-                                   Y, N));
-        GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER,
-                                   CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, Y, N,
-                                   M.p, N));
-        if (mode == GC_ERPA_CHOLESKY_REFINED) {
-          k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, M.p);
-          GC_LAUNCHED(ctx);
-        }
-      }
-      {
-        PhaseScope ph(ctx, GC_PHASE_EIGEN);
-        GC_TRY(eigen(ctx, N, M.p, eig, mode, gemm_precision));
-      }
-      // Y = L U
-      PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
-      GC_CUBLAS(ctx, cublasDtrmm(ctx->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N,
-                                 CUBLAS_DIAG_NON_UNIT, N, N, &one, L.p, N, M.p, N, Y, N));
-    }
-    PhaseScope phn(ctx, GC_PHASE_PRODUCTS);
-    k_norm_chol<<<dim3(ceil_div(N, 256), N), 256, 0, ctx->stream>>>(N, Y, eig);
-    GC_LAUNCHED(ctx);
-    k_sqrt_eig<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(N, eig);
-    GC_LAUNCHED(ctx);
-    return GC_OK;
+    return chol_finish(ctx, N, L.p, M.p, Y, eig, gemm_precision);
   }
   return set_error(ctx, GC_EINVAL, "erpa: unknown mode %d", mode);
+}
+
+int erpa_solve_points(gc_context *ctx, int N, int np, int prec,
+                      const std::function<int(int, double *, double *)> &fill,
+                      const std::function<int(int, const double *, double *)> &use) {
+  if (N <= 0 || np <= 0) return set_error(ctx, GC_EINVAL, "erpa points: N=%d np=%d", N, np);
+  const size_t NN = (size_t)N * N;
+  DevBuf<double> ap, am, T, LM, ev;
+  GC_TRY(ap.alloc(ctx, NN));
+  GC_TRY(am.alloc(ctx, NN));
+  GC_TRY(T.alloc(ctx, NN));
+  GC_TRY(LM.alloc(ctx, 2 * (size_t)np * NN));
+  GC_TRY(ev.alloc(ctx, (size_t)np * N));
+  std::vector<double *> Ls(np), Ms(np), ws(np);
+  for (int k = 0; k < np; ++k) {
+    Ls[k] = LM.p + 2 * (size_t)k * NN;
+    Ms[k] = Ls[k] + NN;
+    ws[k] = ev.p + (size_t)k * N;
+    GC_TRY(fill(k, ap.p, am.p));
+    GC_TRY(erpa_prepare(ctx, N, ap.p, am.p));
+    GC_TRY(chol_form(ctx, N, ap.p, am.p, Ls[k], Ms[k], T.p, GC_ERPA_CHOLESKY_REFINED, prec));
+  }
+  ap.release();
+  am.release();
+  {
+    PhaseScope ph(ctx, GC_PHASE_EIGEN);
+    GC_TRY(eigen_refined_batch(ctx, N, np, Ms.data(), ws.data(), prec));
+  }
+  for (int k = 0; k < np; ++k) {
+    GC_TRY(chol_finish(ctx, N, Ls[k], Ms[k], T.p, ws[k], prec));
+    GC_TRY(use(k, T.p, ws[k]));
+  }
+  return GC_OK;
 }
 
 }  // namespace gc
@@ -1039,6 +1192,12 @@ extern "C" int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns) {
   if (ns > 1000000000ull)
     return gc::set_error(ctx, GC_EINVAL, "pipeline wait limit %llu ns above 1 s", ns);
   ctx->wait_ns = ns ? ns : 1000000000ull;
+  return GC_OK;
+}
+
+extern "C" int gc_set_eig_batch(gc_context *ctx, int on) {
+  if (!ctx) return GC_EINVAL;
+  ctx->eig_batch = on ? 1 : 0;
   return GC_OK;
 }
 

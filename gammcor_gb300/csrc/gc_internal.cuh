@@ -6,6 +6,7 @@
 #include <cusolverDn.h>
 
 #include <cstdarg>
+#include <functional>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -38,6 +39,7 @@ struct gc_context {
   int chol_blocked = 1;              // blocked Cholesky with tensor-core trailing updates
   unsigned long long wait_ns = 1000000000ull;  // limit of the tensor-core GEMMs' pipeline waits
   int oz_tile = 0;  // column tile of the sliced GEMMs: 0 chosen per product, else 64/96/128
+  int eig_batch = 1;  // batch the FP32 eigensolves of a system's points (gc_set_eig_batch)
   cudaEvent_t eig_ev[2] = {nullptr, nullptr};  // around each cuSOLVER eigensolve
   double eig_ms = 0.0;               // device time of the cuSOLVER eigensolves (dsyevd, ssyevd)
   long long eig_calls = 0;
@@ -206,6 +208,14 @@ int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, 
 int erpavec(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig);
 
 // Integrand (gc_integrand.cu).
+// ERPA solutions of np points in the refined Cholesky form with sliced products, the
+// FP32 eigensolves of all points in one batched call: fill(k, ap, am) writes A+B and A-B
+// of point k into the two N x N buffers it is given, use(k, Y, eig) consumes that
+// point's Y (N x N) and omega (N).
+int erpa_solve_points(gc_context *ctx, int N, int np, int prec,
+                      const std::function<int(int, double *, double *)> &fill,
+                      const std::function<int(int, const double *, double *)> &use);
+
 int integrand(gc_context *ctx, const SysDev &sd, const double *eigvec, const double *eig,
               const double *fofo, int precision, double *w_host);
 

@@ -121,6 +121,12 @@ int gc_set_pipeline_wait(gc_context *ctx, unsigned long long ns);
  * (capped at 128 for FP64TC4, 96 for FP64TC5, 64 for FP64TC6). Every width gives
  * the same result bits; only the speed differs. No counterpart in the reference. */
 int gc_set_gemm_tile(gc_context *ctx, int width);
+/* on = 1 (default): the batched AC calls (gc_ac_energy_batched, sessions) solve the FP32
+ * eigenproblems of all lambda points of a system in one batched cuSOLVER call
+ * (cusolverDnXsyevBatched) before refining each, in the GC_ERPA_CHOLESKY_REFINED form
+ * with sliced products; on = 0 solves them one point at a time. Batch workers take the
+ * setting of the context the batched call is given. No counterpart in the reference. */
+int gc_set_eig_batch(gc_context *ctx, int on);
 /* Counters of GC_ERPA_CHOLESKY_REFINED on a context: solves, solves that fell back to
  * dsyevd, and the largest cluster of close eigenvalues diagonalised in a block. */
 int gc_eig_refine_stats(const gc_context *ctx, long long *solves, long long *fallbacks,

@@ -86,3 +86,25 @@ def test_phase_timing_counts_every_phase_and_changes_no_result(golden):
         assert ph[name][1] == 4, (name, ph[name])
     assert ph["products"][1] >= 4
     assert all(ms > 0.0 for ms, _ in ph.values()), ph
+
+
+def test_batched_fp32_eigensolves_match_one_at_a_time(golden):
+    """The FP32 eigensolves of a system's points in one cusolverDnXsyevBatched call (the
+    default) and one ssyevd per point give the same refined energies: both starts are
+    refined to FP64 accuracy, so they agree far inside the 5e-9 Eh bar, and both match
+    the oracle's 8-point energy."""
+    d, batch = golden
+    out = []
+    for on in (True, False):
+        ctx = api.Context(0)
+        try:
+            ctx.set_eig_batch(on)
+            ec, _, wl, st = api.ac_energy_batched(batch, ngrid=8, precision="fp64tc5",
+                                                  erpa_mode="refined", nstreams=2, ctx=ctx)
+        finally:
+            ctx.close()
+        assert st[0] == 0
+        out.append((ec[0], wl[0]))
+    assert abs(out[0][0] - out[1][0]) < 1e-9
+    np.testing.assert_allclose(out[0][1], out[1][1], atol=1e-9)
+    assert abs(out[0][0] - float(d["ecorr8"])) < 5e-9
