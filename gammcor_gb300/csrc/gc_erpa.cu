@@ -757,10 +757,11 @@ __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict_
     const double rl = 1.0 / s[k + k * kCholLd];
     for (int i = k + 1 + t; i < kb; i += blockDim.x) s[i + k * kCholLd] *= rl;
     __syncthreads();
-    const int w = kb - k - 1;
-    for (int e = t; e < w * w; e += blockDim.x) {
-      const int i = k + 1 + e % w, j = k + 1 + e / w;
-      if (i >= j) s[i + j * kCholLd] -= s[i + k * kCholLd] * s[j + k * kCholLd];
+    // trailing lower triangle: lanes along a column (i), the 8 warps over columns (j)
+    const int lane = t & 31, wj = t >> 5;
+    for (int j = k + 1 + wj; j < kb; j += 8) {
+      const double ljk = s[j + k * kCholLd];
+      for (int i = j + lane; i < kb; i += 32) s[i + j * kCholLd] -= s[i + k * kCholLd] * ljk;
     }
     __syncthreads();
   }
