@@ -21,7 +21,10 @@ def test_surrogate_beats_the_method_without_it(gpu_lib):
 def test_gated_energies_equal_the_exact_quadrature(gpu_lib):
     """surrogate.energies with the threshold at zero rejects every prediction: the
     end-node pass plus the interior pass of the batch session must then give the
-    8-point energies of the one-call batch."""
+    8-point energies of the one-call batch. The two passes solve their points' FP32
+    eigenproblems in other batched calls than the one-call batch, so the refinements
+    start from other FP32 vectors and agree to the FP64TC5 products' accuracy (about
+    1e-10 Eh here), checked at 1e-9."""
     import numpy as np
     from gammcor_gb300 import api, synth
     shapes = surrogate.shapes(5, seed=9, nmin=30, nmax=50)
@@ -33,10 +36,13 @@ def test_gated_energies_equal_the_exact_quadrature(gpu_lib):
     assert fb.all() and (st == 0).all()
     ref = api.ac_energy_batched(batch, ngrid=8, precision="fp64tc5", erpa_mode="refined",
                                 nstreams=3)[0]
-    np.testing.assert_allclose(e, ref, atol=1e-10, rtol=0)
+    np.testing.assert_allclose(e, ref, atol=1e-9, rtol=0)
 
 
 def test_session_points_reuse_state_and_validate(gpu_lib):
+    """Points added to a session reuse its integrals and A+-B: E_CAS is identical, and
+    W(lambda) agrees to the FP64TC5 products' accuracy (the points' FP32 eigenproblems
+    are solved in other batched calls, so the refinements start from other vectors)."""
     import numpy as np
     from gammcor_gb300 import api, synth
     from gammcor_gb300._lib import GcError
@@ -54,11 +60,11 @@ def test_session_points_reuse_state_and_validate(gpu_lib):
         w1, ecas1, st1 = ses.points([2, 0], x8[:3])
         w2, ecas2, st2 = ses.points([0, 1, 2, 3], x8)
         assert (st1 == 0).all() and (st2 == 0).all()
-        np.testing.assert_allclose(w2[[2, 0], :3], w1, atol=1e-12, rtol=0)
+        np.testing.assert_allclose(w2[[2, 0], :3], w1, atol=1e-9, rtol=0)
         np.testing.assert_allclose(ecas2[[2, 0]], ecas1, atol=1e-12, rtol=0)
         ref = api.ac_energy_batched(batch, ngrid=8, precision="fp64tc5", erpa_mode="refined",
                                     nstreams=2)
-        np.testing.assert_allclose(w2 @ w8, ref[0], atol=1e-10, rtol=0)
+        np.testing.assert_allclose(w2 @ w8, ref[0], atol=1e-9, rtol=0)
         np.testing.assert_allclose(ecas2, ref[1], atol=1e-10, rtol=0)
         with pytest.raises(GcError):
             ses.points([1, 1], x8[:1])
