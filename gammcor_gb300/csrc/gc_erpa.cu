@@ -773,33 +773,47 @@ __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict_
 }
 
 // Panel solve X L11^T = P for the m x 64 panel P below a factored 64-wide diagonal
-// block L11 (both in the matrix, leading dimension lda), X overwriting P: one thread
-// per row, forward substitution over the 64 columns in registers, L11 in shared
-// memory (row j of L at Ls[64 j ..], read as a broadcast).
-__global__ void __launch_bounds__(32) k_trsm_rows(int m, const double *__restrict__ L11,
-                                                  long long lda, double *__restrict__ P) {
-  __shared__ double Ls[kCholNb * kCholNb];
+// block L11 (both in the matrix, leading dimension lda), X overwriting P. Four lanes
+// share a row, each holding the columns j = q (mod 4) of it in registers; column j is
+// finished by its owner lane, broadcast to the other three by a shuffle and eliminated
+// from their later columns (right-looking). A warp then holds 8 rows, so the FP64 work
+// of a panel is spread over four times as many warps as with one row per thread (GB300's
+// FP64 pipe is narrow and shared by the warps of an SM). L11 sits in shared memory with
+// a padded row stride, read by the four lanes of a row from four banks.
+constexpr int kTrsmRowsPerWarp = 8;
+constexpr int kTrsmWarps = 4;
+__global__ void __launch_bounds__(32 * kTrsmWarps) k_trsm_rows(int m, const double *__restrict__ L11,
+                                                              long long lda,
+                                                              double *__restrict__ P) {
+  __shared__ double Ls[kCholNb * kCholLd];  // Ls[i * kCholLd + j] = L(i, j), j <= i
   __shared__ double rd[kCholNb];
   for (int e = threadIdx.x; e < kCholNb * kCholNb; e += blockDim.x) {
-    const int j = e / kCholNb, k = e % kCholNb;
-    Ls[e] = k <= j ? L11[j + k * lda] : 0.0;
+    const int j = e / kCholNb, i = e % kCholNb;  // coalesced along the column of L11
+    Ls[i * kCholLd + j] = j <= i ? L11[i + j * lda] : 0.0;
   }
   for (int j = threadIdx.x; j < kCholNb; j += blockDim.x) rd[j] = 1.0 / L11[j + j * lda];
   __syncthreads();
-  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (r >= m) return;
-  double x[kCholNb];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, q = lane & 3;
+  const long long r = ((long long)blockIdx.x * kTrsmWarps + warp) * kTrsmRowsPerWarp + (lane >> 2);
+  const bool live = r < m;
+  double acc[kCholNb / 4];
 #pragma unroll
-  for (int j = 0; j < kCholNb; ++j) x[j] = P[r + j * lda];
+  for (int t = 0; t < kCholNb / 4; ++t) acc[t] = live ? P[r + (4 * t + q) * lda] : 0.0;
 #pragma unroll
   for (int j = 0; j < kCholNb; ++j) {
-    double v = x[j];
+    const int t0 = j >> 2, q0 = j & 3;
+    double xj = acc[t0] * rd[j];  // the owner lane's value is the one broadcast
+    xj = __shfl_sync(0xffffffffu, xj, (lane & ~3) | q0);
+    if (q == q0) acc[t0] = xj;
 #pragma unroll
-    for (int k = 0; k < j; ++k) v = fma(-x[k], Ls[j * kCholNb + k], v);
-    x[j] = v * rd[j];
+    for (int t = t0; t < kCholNb / 4; ++t) {
+      const int i = 4 * t + q;
+      if (i > j) acc[t] = fma(-xj, Ls[i * kCholLd + j], acc[t]);
+    }
   }
+  if (live)
 #pragma unroll
-  for (int j = 0; j < kCholNb; ++j) P[r + j * lda] = x[j];
+    for (int t = 0; t < kCholNb / 4; ++t) P[r + (4 * t + q) * lda] = acc[t];
 }
 
 // Cholesky A = L L^T of the lower triangle of A (N x N, column-major) in place, by the
@@ -820,7 +834,8 @@ int chol_blocked(gc_context *ctx, int N, double *A, int prec, int *minor) {
     GC_LAUNCHED(ctx);
     if (m == 0) break;
     double *P = A11 + kb;  // rows k0+kb.., columns k0..k0+kb
-    k_trsm_rows<<<gc::ceil_div(m, 32), 32, 0, ctx->stream>>>(m, A11, lda, P);
+    k_trsm_rows<<<gc::ceil_div(m, kTrsmWarps * kTrsmRowsPerWarp), 32 * kTrsmWarps, 0,
+                  ctx->stream>>>(m, A11, lda, P);
     GC_LAUNCHED(ctx);
     GC_TRY(gc::tc_syrk_sub_lower(ctx, prec, m, kb, P, 1, lda, P + (size_t)kb * lda, lda));
   }

@@ -659,9 +659,37 @@ __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, in
 // n = sum_s a_s 128^(S-1-s), |a_0| <= 128, |a_s| <= 64 otherwise; plane s gets a_s.
 // One FP64 scaling and one conversion per element, the digits in integer arithmetic
 // (the FP64 pipe is the narrow one on this part).
+// x 2^sh rounded to the nearest integer (ties to even), for |x 2^sh| < 2^62, from the bit
+// pattern of x with integer operations only: the same value as __double2ll_rn(ldexp(x, sh))
+// (the scaling is exact unless the result is below 0.5, which rounds to 0 either way),
+// without the FP64 pipe, which is narrow on GB300.
+__device__ __forceinline__ long long scaled_round(double x, int sh) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7ff);
+  unsigned long long m = b & 0xfffffffffffffull;
+  int q = -1074;  // x = +-m 2^q
+  if (E != 0) {
+    m |= 1ull << 52;
+    q = E - 1075;
+  }
+  q += sh;
+  unsigned long long n;
+  if (m == 0 || q < -63) {
+    n = 0;  // |x 2^sh| < 2^53 2^-64 < 1/2
+  } else if (q >= 0) {
+    n = m << q;
+  } else {
+    const int sft = -q;  // 1..63
+    const unsigned long long whole = m >> sft, rem = m & ((1ull << sft) - 1),
+                             half = 1ull << (sft - 1);
+    n = whole + ((rem > half || (rem == half && (whole & 1))) ? 1 : 0);
+  }
+  return (b >> 63) ? -(long long)n : (long long)n;
+}
+
 __device__ __forceinline__ void store_digits(double x, int e, int S, long long plane, long long o,
                                              __nv_bfloat16 *__restrict__ planes) {
-  long long n = e == kBadExp ? 0 : __double2ll_rn(ldexp(x, 7 * S - e));
+  long long n = e == kBadExp ? 0 : scaled_round(x, 7 * S - e);
   for (int s = S - 1; s > 0; --s) {
     const long long d = ((n + 64) & 127) - 64;
     planes[s * plane + o] = __float2bfloat16_rn((float)d);
@@ -671,18 +699,20 @@ __device__ __forceinline__ void store_digits(double x, int e, int S, long long p
 }
 
 // Integer slices: planes[t][b][r][kp] = alpha_t of x[b,r,k] 2^-e[b][r].
+// Rows (b, r) over blockIdx.y, K over the threads: no 64-bit division per element.
 __global__ void k_slice_planes(const double *__restrict__ x, int rows, int K, int Kp, int nb,
                                long long sr, long long sk, long long sb, int S,
                                const int *__restrict__ e, __nv_bfloat16 *__restrict__ planes) {
-  long long plane = (long long)nb * rows * Kp;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < plane;
-       t += (long long)gridDim.x * blockDim.x) {
-    int k = (int)(t % Kp);
-    long long rr = t / Kp;
-    int r = (int)(rr % rows);
-    long long bb = rr / rows;
-    const double xv = k < K ? x[bb * sb + (long long)r * sr + (long long)k * sk] : 0.0;
-    store_digits(xv, e[rr], S, plane, t, planes);
+  const long long plane = (long long)nb * rows * Kp, nrr = (long long)nb * rows;
+  for (long long rr = blockIdx.y; rr < nrr; rr += gridDim.y) {
+    const long long bb = rr / rows;
+    const int r = (int)(rr - bb * rows);
+    const int ex = e[rr];
+    const double *__restrict__ xr = x + bb * sb + (long long)r * sr;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < Kp; k += gridDim.x * blockDim.x) {
+      const double xv = k < K ? xr[(long long)k * sk] : 0.0;
+      store_digits(xv, ex, S, plane, rr * Kp + k, planes);
+    }
   }
 }
 
@@ -922,7 +952,8 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
     GC_LAUNCHED(ctx);
   }
   if (sk == 1) {
-    unsigned grid = std::min<unsigned>(gc::ceil_div(plane, 256), 152u * 32u);
+    const dim3 grid(std::min(gc::ceil_div(op.Kp, 256), 4u),
+                    (unsigned)std::min<long long>((long long)nb * rows, 65535));
     k_slice_planes<<<grid, 256, 0, ctx->stream>>>(x, rows, K, op.Kp, nb, sr, sk, sb, S, op.exps.p,
                                                    op.buf.p);
   } else {
