@@ -80,25 +80,32 @@ __global__ void k_onebody(Geo g, const double *__restrict__ h, const double *__r
 }
 
 // WMAT(k, r) = sum_{l,i,j < nocc} AuxCoeff(k,l,i,j) (kl|ij) RDM2val(i,j,r,l); zero for r >= nocc.
-__global__ void k_wmat(Geo g, const int *__restrict__ grp, const double *__restrict__ fofo,
-                       const double *__restrict__ rv, double lam, double *__restrict__ wmat) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  int r = blockIdx.y;
+// WMAT[k, r] = sum_{i,j,l < nocc} AC(k, l, i, j) (kl|ij) RDM2val(i, j, r, l) for r < nocc
+// is a product Fw RV' with K = nocc^3 (kappa = i + nocc (j + nocc l)):
+//   Fw[k + n kappa] = AC(groups of k, l, i, j) (ij|kl)     (n x K; consecutive k are
+//                                                           consecutive FOFO elements)
+//   RV'[kappa + K r] = RDM2val(i, j, r, l)                  (K x nocc)
+// so it runs as one FP64 DGEMM instead of an nocc^3 loop per element on the CUDA cores.
+__global__ void k_pack_wmat_f(Geo g, const int *__restrict__ grp, const double *__restrict__ fofo,
+                              double lam, double *__restrict__ fw) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= g.n) return;
-  double s = 0.0;
-  if (r < g.nocc) {
-    int gk = grp[k];
-    for (int l = 0; l < g.nocc; ++l) {
-      int gl = grp[l];
-      for (int j = 0; j < g.nocc; ++j) {
-        int gj = grp[j];
-        for (int i = 0; i < g.nocc; ++i)
-          // (kl|ij) read as (ij|kl): consecutive k are consecutive elements of record (i, j)
-          s += AC(g, gk, gl, grp[i], gj, lam) * Fofo(fofo, g, i, j, k, l) * RV(rv, g.nocc, i, j, r, l);
-      }
-    }
+  const int K = g.nocc * g.nocc * g.nocc, gk = grp[k];
+  for (int kappa = blockIdx.y; kappa < K; kappa += gridDim.y) {  // i + nocc (j + nocc l)
+    const int i = kappa % g.nocc, j = (kappa / g.nocc) % g.nocc, l = kappa / (g.nocc * g.nocc);
+    fw[k + (size_t)g.n * kappa] = AC(g, gk, grp[l], grp[i], grp[j], lam) * Fofo(fofo, g, i, j, k, l);
   }
-  wmat[k + (size_t)r * g.n] = s;
+}
+__global__ void k_pack_wmat_rv(int nocc, const double *__restrict__ rv, double *__restrict__ rvp) {
+  const size_t K = (size_t)nocc * nocc * nocc;
+  const size_t total = K * nocc;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t kappa = t % K;
+    const int r = (int)(t / K);
+    const int i = (int)(kappa % nocc), j = (int)((kappa / nocc) % nocc), l = (int)(kappa / ((size_t)nocc * nocc));
+    rvp[t] = RV(rv, nocc, i, j, r, l);
+  }
 }
 
 // E_CAS two-electron part: sum_{ijkl < nocc} RDM2val(i,j,k,l) (ij|kl); per-block partials.
@@ -596,9 +603,22 @@ int assemble_ab(gc_context *ctx, const SysDev &sd, const double *ffoo, const dou
   k_onebody<<<g2, b2, 0, ctx->stream>>>(g, sd.h.p, sd.occ.p, sd.grp.p, fofo, ffoo, alpha, hno.p,
                                         auxi.p, auxio.p);
   GC_LAUNCHED(ctx);
-  k_wmat<<<dim3(ceil_div(n, 128), n), 128, 0, ctx->stream>>>(g, sd.grp.p, fofo, sd.rv.p, alpha,
-                                                             wmat.p);
-  GC_LAUNCHED(ctx);
+  GC_CUDA(ctx, cudaMemsetAsync(wmat.p, 0, (size_t)n * n * sizeof(double), ctx->stream));
+  if (sd.nocc > 0) {
+    const int nocc = sd.nocc, K = nocc * nocc * nocc;
+    DevBuf<double> fw, rvp;
+    GC_TRY(fw.alloc(ctx, (size_t)n * K));
+    GC_TRY(rvp.alloc(ctx, (size_t)K * nocc));
+    k_pack_wmat_f<<<dim3(ceil_div(n, 128), std::min(K, 65535)), 128, 0, ctx->stream>>>(
+        g, sd.grp.p, fofo, alpha, fw.p);
+    GC_LAUNCHED(ctx);
+    k_pack_wmat_rv<<<std::min<unsigned>(ceil_div((size_t)K * nocc, 256), 152u * 8u), 256, 0,
+                     ctx->stream>>>(nocc, sd.rv.p, rvp.p);
+    GC_LAUNCHED(ctx);
+    const double one = 1.0, zero = 0.0;
+    GC_CUBLAS(ctx, cublasDgemm(ctx->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, nocc, K, &one, fw.p, n,
+                               rvp.p, K, &zero, wmat.p, n));
+  }
   Zs Z{Zb.z1.p, Zb.z4.p, Zb.z7.p, Zb.z5.p, Zb.z6.p, Zb.z8.p, Zb.z9.p, Zb.z10.p, Zb.z13.p,
        Zb.z11.p, Zb.z12.p};
   dim3 b3(32, 8), g3(ceil_div(N, 32), ceil_div(N, 8));
