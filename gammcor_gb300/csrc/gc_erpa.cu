@@ -730,44 +730,56 @@ constexpr int kCholNb = 64;
 constexpr int kCholLd = kCholNb + 1;  // padded column stride of the shared block
 
 // Right-looking Cholesky of the kb x kb (kb <= 64) diagonal block A (leading
-// dimension lda) in shared memory; L's lower triangle is written back. A pivot that is
-// not positive (or not finite) records its global order k0 + k + 1 in *info, unless
-// an earlier block already did, and is replaced by 1 so that the rest stays finite.
+// dimension lda) in shared memory; L's lower triangle is written back. The update of
+// step k uses the unscaled column k and the pivot's reciprocal, a_ij -= a_ik a_jk / d_k,
+// and the columns are scaled by 1/sqrt(d_k) at the end, so a step needs one barrier: the
+// thread that updates the next diagonal element forms that pivot's factors right after.
+// A pivot that is not positive (or not finite) records its global order k0 + k + 1 in
+// *info, unless an earlier block already did, and is replaced by 1 so that the rest
+// stays finite.
 __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict__ A, long long lda,
                                                      int k0, int *__restrict__ info) {
   __shared__ double s[kCholNb * kCholLd];
+  __shared__ double rk[kCholNb], sq[kCholNb], isq[kCholNb];  // 1/d, sqrt(d), 1/sqrt(d)
   __shared__ int bad;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, wj = t >> 5;
   for (int e = t; e < kb * kb; e += blockDim.x) {
     const int i = e % kb, j = e / kb;
     s[i + j * kCholLd] = i >= j ? A[i + j * lda] : 0.0;
   }
-  if (t == 0) bad = 0;
+  auto pivot = [&](int k) {
+    double d = s[k + k * kCholLd];
+    if (!(d > 0.0)) {
+      if (!bad) bad = k + 1;
+      d = 1.0;
+    }
+    rk[k] = 1.0 / d;
+    sq[k] = sqrt(d);
+    isq[k] = 1.0 / sq[k];
+  };
   __syncthreads();
-  for (int k = 0; k < kb; ++k) {
-    if (t == 0) {
-      double d = s[k + k * kCholLd];
-      if (!(d > 0.0)) {
-        if (!bad) bad = k + 1;
-        d = 1.0;
-      }
-      s[k + k * kCholLd] = sqrt(d);
-    }
-    __syncthreads();
-    const double rl = 1.0 / s[k + k * kCholLd];
-    for (int i = k + 1 + t; i < kb; i += blockDim.x) s[i + k * kCholLd] *= rl;
-    __syncthreads();
-    // trailing lower triangle: lanes along a column (i), the 8 warps over columns (j)
-    const int lane = t & 31, wj = t >> 5;
+  if (t == 0) {
+    bad = 0;
+    pivot(0);
+  }
+  __syncthreads();
+  for (int k = 0; k + 1 < kb; ++k) {
+    const double r = rk[k];
+    // trailing lower triangle: the 8 warps over columns j, lanes along them; thread 0
+    // (warp 0, lane 0) updates the next diagonal element (k + 1, k + 1) first
     for (int j = k + 1 + wj; j < kb; j += 8) {
-      const double ljk = s[j + k * kCholLd];
-      for (int i = j + lane; i < kb; i += 32) s[i + j * kCholLd] -= s[i + k * kCholLd] * ljk;
+      const double tj = s[j + k * kCholLd] * r;
+      for (int i = j + lane; i < kb; i += 32) s[i + j * kCholLd] -= s[i + k * kCholLd] * tj;
     }
+    if (t == 0) pivot(k + 1);
     __syncthreads();
   }
   for (int e = t; e < kb * kb; e += blockDim.x) {
     const int i = e % kb, j = e / kb;
-    if (i >= j) A[i + j * lda] = s[i + j * kCholLd];
+    if (i > j)
+      A[i + j * lda] = s[i + j * kCholLd] * isq[j];
+    else if (i == j)
+      A[i + j * lda] = sq[j];
   }
   if (t == 0 && bad && *info == 0) *info = k0 + bad;
 }
