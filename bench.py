@@ -492,8 +492,10 @@ def run_ours(args):
     ctx.set_phase_timing(False)
     eig = {"device_ms_per_step": (eig1[0] - eig0[0]) / args.steps,
            "calls_per_step": (eig1[1] - eig0[1]) // args.steps,
-           "what": "cuSOLVER eigensolves (ssyevd of the refined form, dsyevd fallbacks), CUDA "
-                   "events around each call, summed over the concurrent worker streams"}
+           "what": "cuSOLVER FP32 eigensolves of the refined form (one cusolverDnXsyevBatched "
+                   "call per system for all its points; ssyevd / dsyevd fallbacks), CUDA events "
+                   "around each call, summed over the concurrent worker streams; calls = "
+                   "matrices solved"}
     phases = {k: {"device_ms_per_step": (ph1[k][0] - ph0[k][0]) / args.steps,
                   "calls_per_step": (ph1[k][1] - ph0[k][1]) // args.steps} for k in ph1}
     phases["what"] = ("CUDA events around each phase on its worker stream, summed over the "
