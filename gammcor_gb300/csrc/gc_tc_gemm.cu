@@ -630,35 +630,58 @@ __global__ void __launch_bounds__(oz_threads(TBN), 1)
   }
 }
 
-// Row exponents: e[b][r] = 1 + ilogb(max_k |x[b,r,k]|) (0 for a zero row,
-// kBadExp for a row with a non-finite element).
+// |x| as its bit pattern without the sign: for finite values the unsigned integer order is
+// the order of |x|, and a value with the exponent field all ones is an infinity or a NaN.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+// 1 + ilogb of the value whose |x| bits are m (m > 0, finite), from the bits.
+__device__ __forceinline__ int exp_of_bits(unsigned long long m) {
+  const int E = (int)(m >> 52);
+  return E > 0 ? E - 1022 : -1010 - __clzll((long long)m);
+}
+constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
+
+// Row exponents: e[b][r] = 1 + ilogb(max_k |x[b,r,k]|) (0 for a zero row, kBadExp for a
+// row with a non-finite element), with integer operations on the bit patterns (no FP64
+// pipe): one warp per row (rows whose K elements are contiguous, sk = 1) ...
 __global__ void k_row_exponent(const double *__restrict__ x, int rows, int K, int nb, long long sr,
                                long long sk, long long sb, int *__restrict__ e) {
   long long total = (long long)nb * rows;
-  // one warp per row
   long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / 32;
   int lane = threadIdx.x % 32;
   for (long long t = wid; t < total; t += (long long)gridDim.x * blockDim.x / 32) {
     int r = (int)(t % rows);
     long long bb = t / rows;
     const double *row = x + bb * sb + (long long)r * sr;
-    double mx = 0.0;
-    bool bad = false;
-    for (int k = lane; k < K; k += 32) {
-      const double v = row[(long long)k * sk];
-      bad |= !isfinite(v);
-      mx = fmax(mx, fabs(v));
-    }
-    for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, off));
-    bad = __any_sync(0xffffffffu, bad);
-    if (lane == 0) e[t] = bad ? kBadExp : (mx > 0.0 ? ilogb(mx) + 1 : 0);
+    unsigned long long mx = 0;
+    for (int k = lane; k < K; k += 32) mx = max(mx, abs_bits(row[(long long)k * sk]));
+    for (int off = 16; off > 0; off >>= 1) mx = max(mx, __shfl_down_sync(0xffffffffu, mx, off));
+    if (lane == 0) e[t] = mx >= kInfBits ? kBadExp : (mx ? exp_of_bits(mx) : 0);
   }
 }
 
-// Balanced base-128 digits of n = rint(x 2^(7S - e)) (|n| < 2^(7S) since |x| < 2^e):
-// n = sum_s a_s 128^(S-1-s), |a_0| <= 128, |a_s| <= 64 otherwise; plane s gets a_s.
-// One FP64 scaling and one conversion per element, the digits in integer arithmetic
-// (the FP64 pipe is the narrow one on this part).
+// ... or, for consecutive rows contiguous (sr = 1), 32 rows per block with the lanes along
+// the rows (loads coalesced for every k) and 8 warps splitting K.
+__global__ void k_row_exponent_cols(const double *__restrict__ x, int rows, int K,
+                                    long long sk, long long sb, int *__restrict__ e) {
+  __shared__ unsigned long long part[8][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int r = blockIdx.x * 32 + tx;
+  const long long bb = blockIdx.y;
+  unsigned long long mx = 0;
+  if (r < rows) {
+    const double *row = x + bb * sb + r;
+    for (int k = ty; k < K; k += 8) mx = max(mx, abs_bits(row[(long long)k * sk]));
+  }
+  part[ty][tx] = mx;
+  __syncthreads();
+  if (ty == 0 && r < rows) {
+    for (int w = 1; w < 8; ++w) mx = max(mx, part[w][tx]);
+    e[bb * rows + r] = mx >= kInfBits ? kBadExp : (mx ? exp_of_bits(mx) : 0);
+  }
+}
+
 // x 2^sh rounded to the nearest integer (ties to even), for |x 2^sh| < 2^62, from the bit
 // pattern of x with integer operations only: the same value as __double2ll_rn(ldexp(x, sh))
 // (the scaling is exact unless the result is below 0.5, which rounds to 0 either way),
@@ -687,6 +710,9 @@ __device__ __forceinline__ long long scaled_round(double x, int sh) {
   return (b >> 63) ? -(long long)n : (long long)n;
 }
 
+// Balanced base-128 digits of n = rint(x 2^(7S - e)) (|n| < 2^(7S) since |x| < 2^e):
+// n = sum_s a_s 128^(S-1-s), |a_0| <= 128, |a_s| <= 64 otherwise; plane s gets a_s. All
+// in integer arithmetic.
 __device__ __forceinline__ void store_digits(double x, int e, int S, long long plane, long long o,
                                              __nv_bfloat16 *__restrict__ planes) {
   long long n = e == kBadExp ? 0 : scaled_round(x, 7 * S - e);
@@ -945,7 +971,11 @@ int make_oz_operand(gc_context *ctx, OzOperand &op, const double *x, int rows, i
   size_t plane = (size_t)nb * rows * op.Kp;
   GC_TRY(op.exps.alloc(ctx, (size_t)nb * rows));
   GC_TRY(op.buf.alloc(ctx, plane * S));
-  {
+  if (sr == 1 && sk != 1 && nb <= 65535) {
+    k_row_exponent_cols<<<dim3(gc::ceil_div(rows, 32), nb), dim3(32, 8), 0, ctx->stream>>>(
+        x, rows, K, sk, sb, op.exps.p);
+    GC_LAUNCHED(ctx);
+  } else {
     size_t warps = (size_t)nb * rows;
     unsigned grid = std::min<unsigned>(gc::ceil_div(warps * 32, 256), 152u * 64u);
     k_row_exponent<<<grid, 256, 0, ctx->stream>>>(x, rows, K, nb, sr, sk, sb, op.exps.p);
