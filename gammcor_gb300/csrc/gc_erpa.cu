@@ -732,8 +732,10 @@ constexpr int kCholLd = kCholNb + 1;  // padded column stride of the shared bloc
 // Right-looking Cholesky of the kb x kb (kb <= 64) diagonal block A (leading
 // dimension lda) in shared memory; L's lower triangle is written back. The update of
 // step k uses the unscaled column k and the pivot's reciprocal, a_ij -= a_ik a_jk / d_k,
-// and the columns are scaled by 1/sqrt(d_k) at the end, so a step needs one barrier: the
-// thread that updates the next diagonal element forms that pivot's factors right after.
+// and the columns are scaled by 1/sqrt(d_k) at the end, so a step needs one barrier.
+// Thread 0 updates the next diagonal element and forms that pivot's factors (one FP64
+// square root and one division) while warps 1-7 update the rest of the trailing
+// triangle: the pivot's latency, not the FP64 work of one SM, set the time of a step.
 // A pivot that is not positive (or not finite) records its global order k0 + k + 1 in
 // *info, unless an earlier block already did, and is replaced by 1 so that the rest
 // stays finite.
@@ -742,7 +744,7 @@ __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict_
   __shared__ double s[kCholNb * kCholLd];
   __shared__ double rk[kCholNb], sq[kCholNb], isq[kCholNb];  // 1/d, sqrt(d), 1/sqrt(d)
   __shared__ int bad;
-  const int t = threadIdx.x, lane = t & 31, wj = t >> 5;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   for (int e = t; e < kb * kb; e += blockDim.x) {
     const int i = e % kb, j = e / kb;
     s[i + j * kCholLd] = i >= j ? A[i + j * lda] : 0.0;
@@ -753,9 +755,10 @@ __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict_
       if (!bad) bad = k + 1;
       d = 1.0;
     }
-    rk[k] = 1.0 / d;
-    sq[k] = sqrt(d);
-    isq[k] = 1.0 / sq[k];
+    const double is = 1.0 / sqrt(d);
+    isq[k] = is;
+    sq[k] = d * is;
+    rk[k] = is * is;
   };
   __syncthreads();
   if (t == 0) {
@@ -765,13 +768,18 @@ __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict_
   __syncthreads();
   for (int k = 0; k + 1 < kb; ++k) {
     const double r = rk[k];
-    // trailing lower triangle: the 8 warps over columns j, lanes along them; thread 0
-    // (warp 0, lane 0) updates the next diagonal element (k + 1, k + 1) first
-    for (int j = k + 1 + wj; j < kb; j += 8) {
-      const double tj = s[j + k * kCholLd] * r;
-      for (int i = j + lane; i < kb; i += 32) s[i + j * kCholLd] -= s[i + k * kCholLd] * tj;
+    if (t == 0) {  // the next diagonal element, then its pivot
+      const double akk = s[(k + 1) + k * kCholLd];
+      s[(k + 1) + (k + 1) * kCholLd] -= akk * (akk * r);
+      pivot(k + 1);
+    } else if (warp > 0) {
+      // the rest of the trailing lower triangle: warps 1-7 over columns j, lanes along them
+      for (int j = k + warp; j < kb; j += 7) {
+        const double tj = s[j + k * kCholLd] * r;
+        for (int i = j + lane; i < kb; i += 32)
+          if (i != k + 1) s[i + j * kCholLd] -= s[i + k * kCholLd] * tj;
+      }
     }
-    if (t == 0) pivot(k + 1);
     __syncthreads();
   }
   for (int e = t; e < kb * kb; e += blockDim.x) {
