@@ -740,7 +740,11 @@ constexpr int kCholLd = kCholNb + 1;  // padded column stride of the shared bloc
 // *info, unless an earlier block already did, and is replaced by 1 so that the rest
 // stays finite.
 __global__ void __launch_bounds__(256) k_potrf_block(int kb, double *__restrict__ A, long long lda,
-                                                     int k0, int *__restrict__ info) {
+                                                     int k0, int *__restrict__ info,
+                                                     long long sb) {
+  // one CTA per matrix of a batch (A and info of matrix b at b * sb and b)
+  A += blockIdx.x * sb;
+  info += blockIdx.x;
   __shared__ double s[kCholNb * kCholLd];
   __shared__ double rk[kCholNb], sq[kCholNb], isq[kCholNb];  // 1/d, sqrt(d), 1/sqrt(d)
   __shared__ int bad;
@@ -804,7 +808,10 @@ constexpr int kTrsmRowsPerWarp = 8;
 constexpr int kTrsmWarps = 4;
 __global__ void __launch_bounds__(32 * kTrsmWarps) k_trsm_rows(int m, const double *__restrict__ L11,
                                                               long long lda,
-                                                              double *__restrict__ P) {
+                                                              double *__restrict__ P,
+                                                              long long sb) {
+  L11 += blockIdx.y * sb;  // matrix blockIdx.y of a batch
+  P += blockIdx.y * sb;
   __shared__ double Ls[kCholNb * kCholLd];  // Ls[i * kCholLd + j] = L(i, j), j <= i
   __shared__ double rd[kCholNb];
   for (int e = threadIdx.x; e < kCholNb * kCholNb; e += blockDim.x) {
@@ -836,34 +843,40 @@ __global__ void __launch_bounds__(32 * kTrsmWarps) k_trsm_rows(int m, const doub
     for (int t = 0; t < kCholNb / 4; ++t) P[r + (4 * t + q) * lda] = acc[t];
 }
 
-// Cholesky A = L L^T of the lower triangle of A (N x N, column-major) in place, by the
-// kernels above and FP64-accurate products of precision prec (L L^T equals A to that
-// product's ~2^-35 relative error; the diagonal blocks and panels are FP64). The strict
-// upper triangle is left as it was. *minor = 0 on success, else the order of the first
-// leading minor that is not positive definite.
-int chol_blocked(gc_context *ctx, int N, double *A, int prec, int *minor) {
-  *minor = 0;
+// Cholesky A = L L^T of the lower triangles of nmat N x N matrices (column-major, matrix
+// b at A + b*sb) in place, by the kernels above and FP64-accurate products of precision
+// prec (L L^T equals A to that product's ~2^-35 relative error; the diagonal blocks and
+// panels are FP64). The matrices of a batch go through the 64-wide steps together: one
+// launch per kernel and step for all of them. The strict upper triangles are left as they
+// were. minor[b] = 0 on success, else the order of the first leading minor of matrix b
+// that is not positive definite.
+int chol_blocked_batch(gc_context *ctx, int N, int nmat, double *A, long long sb, int prec,
+                       int *minor) {
   const long long lda = N;
   gc::DevBuf<int> info;
-  GC_TRY(info.alloc(ctx, 1));
-  GC_CUDA(ctx, cudaMemsetAsync(info.p, 0, sizeof(int), ctx->stream));
+  GC_TRY(info.alloc(ctx, nmat));
+  GC_CUDA(ctx, cudaMemsetAsync(info.p, 0, nmat * sizeof(int), ctx->stream));
   for (int k0 = 0; k0 < N; k0 += kCholNb) {
     const int kb = std::min(kCholNb, N - k0), m = N - k0 - kb;
     double *A11 = A + k0 + (size_t)k0 * lda;
-    k_potrf_block<<<1, 256, 0, ctx->stream>>>(kb, A11, lda, k0, info.p);
+    k_potrf_block<<<nmat, 256, 0, ctx->stream>>>(kb, A11, lda, k0, info.p, sb);
     GC_LAUNCHED(ctx);
     if (m == 0) break;
     double *P = A11 + kb;  // rows k0+kb.., columns k0..k0+kb
-    k_trsm_rows<<<gc::ceil_div(m, kTrsmWarps * kTrsmRowsPerWarp), 32 * kTrsmWarps, 0,
-                  ctx->stream>>>(m, A11, lda, P);
+    k_trsm_rows<<<dim3(gc::ceil_div(m, kTrsmWarps * kTrsmRowsPerWarp), nmat), 32 * kTrsmWarps, 0,
+                  ctx->stream>>>(m, A11, lda, P, sb);
     GC_LAUNCHED(ctx);
-    GC_TRY(gc::tc_syrk_sub_lower(ctx, prec, m, kb, P, 1, lda, P + (size_t)kb * lda, lda));
+    GC_TRY(gc::tc_syrk_sub_lower(ctx, prec, m, kb, P, 1, lda, P + (size_t)kb * lda, lda, nmat, sb));
   }
-  int h = 0;
-  GC_CUDA(ctx, cudaMemcpyAsync(&h, info.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaMemcpyAsync(minor, info.p, nmat * sizeof(int), cudaMemcpyDeviceToHost,
+                               ctx->stream));
   GC_TRY(gc::check_flag(ctx));  // synchronises; covers the trailing-update GEMMs
-  *minor = h;
   return GC_OK;
+}
+
+// One matrix: *minor as minor[0] above.
+int chol_blocked(gc_context *ctx, int N, double *A, int prec, int *minor) {
+  return chol_blocked_batch(ctx, N, 1, A, 0, prec, minor);
 }
 
 // Eigenpairs of the symmetric M in place (vectors overwrite M, values in w):
@@ -1139,16 +1152,46 @@ int erpa_solve_points(gc_context *ctx, int N, int np, int prec,
   GC_TRY(LM.alloc(ctx, 2 * (size_t)np * NN));
   GC_TRY(ev.alloc(ctx, (size_t)np * N));
   std::vector<double *> Ls(np), Ms(np), ws(np);
+  // A+-B of every point: A+B into the L slot, A-B into the M slot
   for (int k = 0; k < np; ++k) {
     Ls[k] = LM.p + 2 * (size_t)k * NN;
     Ms[k] = Ls[k] + NN;
     ws[k] = ev.p + (size_t)k * N;
     GC_TRY(fill(k, ap.p, am.p));
     GC_TRY(erpa_prepare(ctx, N, ap.p, am.p));
-    GC_TRY(chol_form(ctx, N, ap.p, am.p, Ls[k], Ms[k], T.p, GC_ERPA_CHOLESKY_REFINED, prec));
+    GC_CUDA(ctx, cudaMemcpyAsync(Ls[k], ap.p, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+    GC_CUDA(ctx, cudaMemcpyAsync(Ms[k], am.p, NN * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
   }
   ap.release();
   am.release();
+  const dim3 b2(32, 8), g2(ceil_div(N, 32), ceil_div(N, 8));
+  {
+    // the Cholesky factors of all points, the 64-wide steps batched over the points
+    PhaseScope ph(ctx, GC_PHASE_CHOLESKY);
+    std::vector<int> minor(np, 0);
+    if (gc::is_sliced(prec) && ctx->chol_blocked)
+      GC_TRY(chol_blocked_batch(ctx, N, np, LM.p, 2 * (long long)NN, prec, minor.data()));
+    else
+      for (int k = 0; k < np; ++k) GC_TRY(chol_plain(ctx, N, Ls[k], &minor[k]));
+    for (int k = 0; k < np; ++k)
+      if (minor[k] > 0)
+        return set_error(ctx, GC_ENOTPD, "A+B is not positive definite (potrf minor %d)",
+                         minor[k]);
+    for (int k = 0; k < np; ++k) {
+      k_zero_upper<<<g2, b2, 0, ctx->stream>>>(N, Ls[k]);
+      GC_LAUNCHED(ctx);
+    }
+  }
+  for (int k = 0; k < np; ++k) {
+    // M = L^T (A- L): T = A- L, then M (which held A-) = L^T T
+    PhaseScope ph(ctx, GC_PHASE_PRODUCTS);
+    GC_TRY(product(ctx, prec, false, N, N, N, Ms[k], N, Ls[k], N, T.p, N));
+    GC_TRY(product(ctx, prec, true, N, N, N, Ls[k], N, T.p, N, Ms[k], N));
+    k_symmetrize<<<g2, b2, 0, ctx->stream>>>(N, Ms[k]);
+    GC_LAUNCHED(ctx);
+  }
   {
     PhaseScope ph(ctx, GC_PHASE_EIGEN);
     GC_TRY(eigen_refined_batch(ctx, N, np, Ms.data(), ws.data(), prec));

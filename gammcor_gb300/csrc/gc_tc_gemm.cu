@@ -1197,15 +1197,15 @@ int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, c
 }
 
 int tc_syrk_sub_lower(gc_context *ctx, int precision, int M, int K, const double *P, long long sm,
-                      long long sk, double *C, long long ldc) {
+                      long long sk, double *C, long long ldc, int nbatch, long long sb) {
   if (!is_oz(precision))
     return set_error(ctx, GC_EINVAL, "syrk_sub_lower: needs a sliced FP64-accurate precision");
   OzPlan pl = oz_plan(precision);
   OzOperand a, b;
-  GC_TRY(make_oz_operand(ctx, a, P, M, K, 1, sm, sk, 0, pl.S, BM));
-  GC_TRY(alias_oz_operand(ctx, a, b, oz_tile(ctx, pl.S, M, M, 1)));
-  OzEpi e{2, C, ldc, 0, nullptr, nullptr, nullptr, nullptr, 0, 0, M};
-  GC_TRY(run_oz(ctx, a, b, M, M, 1, pl, e));
+  GC_TRY(make_oz_operand(ctx, a, P, M, K, nbatch, sm, sk, sb, pl.S, BM));
+  GC_TRY(alias_oz_operand(ctx, a, b, oz_tile(ctx, pl.S, M, M, nbatch)));
+  OzEpi e{2, C, ldc, nbatch > 1 ? sb : 0, nullptr, nullptr, nullptr, nullptr, 0, 0, M};
+  GC_TRY(run_oz(ctx, a, b, M, M, nbatch, pl, e));
   return GC_OK;  // the device flag is read at the caller's next sync point
 }
 

@@ -42,9 +42,10 @@ int tc_gemm_strided_lower(gc_context *ctx, int precision, int M, int N, int K, c
 
 // C[m + n*ldc] -= sum_k P(m,k) P(n,k) for m >= n (the lower triangle of an M x M
 // C, diagonal included) with P(m,k) = P[m*sm + k*sk], on the sliced path; the
-// strict upper triangle of C is not touched.
+// strict upper triangle of C is not touched. nbatch products, P and C of batch b at
+// b*sb from the base pointers.
 int tc_syrk_sub_lower(gc_context *ctx, int precision, int M, int K, const double *P, long long sm,
-                      long long sk, double *C, long long ldc);
+                      long long sk, double *C, long long ldc, int nbatch = 1, long long sb = 0);
 
 int fp64_two_sided(gc_context *ctx, int n, int cnt, const double *M, int nX, const double *CX,
                    int nY, const double *CY, double *T1, double *out, long long ostride);
