@@ -221,3 +221,28 @@ def test_cholesky_reports_not_positive_definite(gpu_lib):
         assert ei.value.code == 5  # GC_ENOTPD
         minors.append(int(str(ei.value).split("minor")[1].strip(" )")))
     assert minors[0] == minors[1] > 0
+
+
+def test_batch_reports_the_system_without_a_cholesky_factor(batch3):
+    """A system whose A+B is not positive definite goes through the batched Cholesky of
+    its points beside the others: its status is GC_ENOTPD, and the other systems'
+    energies still match the oracle."""
+    from gammcor_gb300 import synth
+    batch, refs = batch3
+    bad = synth.make_system(n=18, nin=3, nact=4, rank=72, seed=1, eri_scale=0.25)
+    G, ffoo, fofo = oracle_integrals(bad)
+    indn = R.pair_space(bad.occ, bad.nele)
+    x, _ = R.gauleg(0.0, 1.0, 8)
+    not_pd = []
+    for lam in x:
+        abp, _, _ = R.ab_cas_fofo(bad.occ, bad.xone, np.eye(bad.n), indn, bad.nin, bad.nact, ffoo,
+                                  fofo, bad.rdm2act, lam)
+        not_pd.append(np.linalg.eigvalsh(0.5 * (abp + abp.T)).min() <= 0.0)
+    assert any(not_pd)  # the case this test is about
+    mixed = api.BatchInputs([batch.systems[0], bad, batch.systems[2]], DEV)
+    ecorr, ecas, wl, status = api.ac_energy_batched(mixed, ngrid=8, precision="fp64tc5",
+                                                    erpa_mode="refined", nstreams=2)
+    assert status[1] == 5  # GC_ENOTPD
+    assert status[0] == 0 and status[2] == 0
+    assert abs(ecorr[0] - refs[0][1]) < 5e-9
+    assert abs(ecorr[2] - refs[2][1]) < 5e-9
