@@ -82,8 +82,8 @@ def test_phase_timing_counts_every_phase_and_changes_no_result(golden):
     assert e_on[0] == e_off[0]
     assert ph["transform"][1] == 2                # FOFO and FFOO
     assert ph["assembly"][1] == 2 + 4             # A+-B at 0 and 1, one combination per point
-    for name in ("cholesky", "integrand"):
-        assert ph[name][1] == 4, (name, ph[name])
+    assert ph["integrand"][1] == 4
+    assert ph["cholesky"][1] == 1                 # the four points' factors in one batch
     assert ph["eigen"][1] == 1                    # the four points' FP32 solves in one batch
     assert ph["products"][1] >= 4
     assert all(ms > 0.0 for ms, _ in ph.values()), ph
