@@ -902,74 +902,91 @@ __global__ void k_ascending(int N, int np, const float *__restrict__ w, int *__r
     if (!isfinite(wk[i]) || (i + 1 < N && !(wk[i] <= wk[i + 1]))) bad[k] = 1;
 }
 
-// Eigenpairs of np symmetric N x N matrices M[k] in place (vectors overwrite M[k], values
-// in w[k]) in the refined form: one batched FP32 eigensolve (cusolverDnXsyevBatched) for
-// all of them, then the refinement of each. Concurrent FP32 eigensolves of one order
-// overlap poorly on separate streams; the batched solver runs them 2-4x faster. A
-// matrix whose FP32 solve failed, or whose refinement cannot proceed, is solved alone
-// (ssyevd start, then dsyevd), as eigen() does.
-int eigen_refined_batch(gc_context *ctx, int N, int np, double *const *M, double *const *w,
-                        int prec) {
-  if (np == 1 || N > 65535) {
-    for (int k = 0; k < np; ++k) GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
-    return GC_OK;
-  }
+// The batched FP32 start of eigen_refined_batch: m32 (np x N x N) receives the FP32
+// eigenvectors of the M[k], h (2 np) the solver status of each matrix and then whether its
+// eigenvalues are not finite and ascending.
+int fp32_batch_start(gc_context *ctx, int N, int np, double *const *M, gc::DevBuf<float> &m32,
+                     std::vector<int> &h) {
   const size_t NN = (size_t)N * N;
-  gc::DevBuf<float> m32, w32;
+  gc::DevBuf<float> w32;
   gc::DevBuf<int> info;
   GC_TRY(m32.alloc(ctx, NN * np));
   GC_TRY(w32.alloc(ctx, (size_t)N * np));
-  GC_TRY(info.alloc(ctx, 2 * (size_t)np));  // solver status, then the ascending check
+  GC_TRY(info.alloc(ctx, 2 * (size_t)np));
   const unsigned ew = std::min<size_t>(gc::ceil_div(NN, 256), 152 * 16);
   for (int k = 0; k < np; ++k) {
     k_d2f<<<ew, 256, 0, ctx->stream>>>(NN, M[k], m32.p + k * NN);
     GC_LAUNCHED(ctx);
   }
   GC_CUDA(ctx, cudaMemsetAsync(info.p, 0, 2 * (size_t)np * sizeof(int), ctx->stream));
-  {
-    cusolverDnParams_t params = nullptr;
-    GC_CUSOLVER(ctx, cusolverDnCreateParams(&params));
-    struct ParamsGuard {
-      cusolverDnParams_t p;
-      ~ParamsGuard() { cusolverDnDestroyParams(p); }
-    } guard{params};
-    size_t wd = 0, wh = 0;
-    GC_CUSOLVER(ctx, cusolverDnXsyevBatched_bufferSize(
-                         ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N,
-                         CUDA_R_32F, m32.p, N, CUDA_R_32F, w32.p, CUDA_R_32F, &wd, &wh, np));
-    gc::DevBuf<char> work;
-    GC_TRY(work.alloc(ctx, std::max<size_t>(wd, 1)));
-    std::vector<char> hwork(std::max<size_t>(wh, 1));
-    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[0], ctx->stream));
-    GC_CUSOLVER(ctx, cusolverDnXsyevBatched(ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR,
-                                            CUBLAS_FILL_MODE_LOWER, N, CUDA_R_32F, m32.p, N,
-                                            CUDA_R_32F, w32.p, CUDA_R_32F, work.p, wd,
-                                            hwork.data(), wh, info.p, np));
-    GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[1], ctx->stream));
-    k_ascending<<<dim3(gc::ceil_div(N, 256), np), 256, 0, ctx->stream>>>(N, np, w32.p,
-                                                                         info.p + np);
-    GC_LAUNCHED(ctx);
-    std::vector<int> h(2 * (size_t)np);
-    GC_CUDA(ctx, cudaMemcpyAsync(h.data(), info.p, 2 * (size_t)np * sizeof(int),
-                                 cudaMemcpyDeviceToHost, ctx->stream));
-    GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    float ms = 0.f;
-    GC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->eig_ev[0], ctx->eig_ev[1]));
-    ctx->eig_ms += ms;
-    ctx->eig_calls += np;
-    w32.release();
-    for (int k = 0; k < np; ++k) {
-      if (h[k] != 0 || h[np + k] != 0) {  // solved alone: the ssyevd start, then dsyevd
-        GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
-        continue;
-      }
-      ctx->refine_solves++;
-      bool fallback = false;
-      GC_TRY(refine_from_fp32(ctx, N, prec, M[k], m32.p + k * NN, M[k], w[k], &fallback));
-      if (fallback) {
-        ctx->refine_fallbacks++;
-        GC_TRY(syevd(ctx, N, M[k], w[k]));
-      }
+  cusolverDnParams_t params = nullptr;
+  GC_CUSOLVER(ctx, cusolverDnCreateParams(&params));
+  struct ParamsGuard {
+    cusolverDnParams_t p;
+    ~ParamsGuard() { cusolverDnDestroyParams(p); }
+  } guard{params};
+  size_t wd = 0, wh = 0;
+  GC_CUSOLVER(ctx, cusolverDnXsyevBatched_bufferSize(
+                       ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N,
+                       CUDA_R_32F, m32.p, N, CUDA_R_32F, w32.p, CUDA_R_32F, &wd, &wh, np));
+  gc::DevBuf<char> work;
+  GC_TRY(work.alloc(ctx, std::max<size_t>(wd, 1)));
+  std::vector<char> hwork(std::max<size_t>(wh, 1));
+  GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[0], ctx->stream));
+  GC_CUSOLVER(ctx, cusolverDnXsyevBatched(ctx->cusolver, params, CUSOLVER_EIG_MODE_VECTOR,
+                                          CUBLAS_FILL_MODE_LOWER, N, CUDA_R_32F, m32.p, N,
+                                          CUDA_R_32F, w32.p, CUDA_R_32F, work.p, wd, hwork.data(),
+                                          wh, info.p, np));
+  GC_CUDA(ctx, cudaEventRecord(ctx->eig_ev[1], ctx->stream));
+  k_ascending<<<dim3(gc::ceil_div(N, 256), np), 256, 0, ctx->stream>>>(N, np, w32.p, info.p + np);
+  GC_LAUNCHED(ctx);
+  h.assign(2 * (size_t)np, 0);
+  GC_CUDA(ctx, cudaMemcpyAsync(h.data(), info.p, 2 * (size_t)np * sizeof(int),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  GC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  GC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->eig_ev[0], ctx->eig_ev[1]));
+  ctx->eig_ms += ms;
+  ctx->eig_calls += np;
+  return GC_OK;
+}
+
+// Eigenpairs of np symmetric N x N matrices M[k] in place (vectors overwrite M[k], values
+// in w[k]) in the refined form: one batched FP32 eigensolve (cusolverDnXsyevBatched) for
+// all of them, then the refinement of each. Concurrent FP32 eigensolves of one order
+// overlap poorly on separate streams; the batched solver runs them 2-4x faster. A
+// matrix whose FP32 solve failed, or whose refinement cannot proceed, is solved alone
+// (ssyevd start, then dsyevd), as eigen() does; so are all of them when the batched
+// solver refuses the order or its workspace does not fit.
+int eigen_refined_batch(gc_context *ctx, int N, int np, double *const *M, double *const *w,
+                        int prec) {
+  auto one_by_one = [&]() -> int {
+    for (int k = 0; k < np; ++k) GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
+    return GC_OK;
+  };
+  if (np == 1 || N > 65535) return one_by_one();
+  const size_t NN = (size_t)N * N;
+  gc::DevBuf<float> m32;
+  std::vector<int> h;
+  const int r = fp32_batch_start(ctx, N, np, M, m32, h);
+  if (r == GC_ECUSOLVER || r == GC_ENOMEM) {
+    // the batched solver refused this order or batch, or its workspace does not fit:
+    // the points are solved one at a time
+    m32.release();
+    return one_by_one();
+  }
+  GC_TRY(r);
+  for (int k = 0; k < np; ++k) {
+    if (h[k] != 0 || h[np + k] != 0) {  // solved alone: the ssyevd start, then dsyevd
+      GC_TRY(eigen(ctx, N, M[k], w[k], GC_ERPA_CHOLESKY_REFINED, prec));
+      continue;
+    }
+    ctx->refine_solves++;
+    bool fallback = false;
+    GC_TRY(refine_from_fp32(ctx, N, prec, M[k], m32.p + k * NN, M[k], w[k], &fallback));
+    if (fallback) {
+      ctx->refine_fallbacks++;
+      GC_TRY(syevd(ctx, N, M[k], w[k]));
     }
   }
   return GC_OK;
