@@ -513,9 +513,14 @@ def run_ours(args):
     # point) on the whole batch with the same worker streams, timed with CUDA events; every
     # energy of the last timed step is checked against it.
     plain = None
+    key = np.array([args.nsys, args.seed, args.ngrid, rank], dtype=np.int64)
     cached = args.plain_energies and Path(args.plain_energies).exists()
-    if not args.no_subset and cached:
+    if cached:
         d = np.load(args.plain_energies)
+        if "key" not in d or not np.array_equal(d["key"], key):
+            raise SystemExit(f"{args.plain_energies} holds plain energies of another workload "
+                             "(systems, seed, points or rank differ)")
+    if not args.no_subset and cached:
         pe, pst, t_plain, pclk = d["ecorr"], d["status"], float(d["ms"]), None
     elif not args.no_subset:
         pl = dict(ngrid=args.ngrid, precision="fp64", erpa_mode="symm1", affine=False,
@@ -529,7 +534,7 @@ def run_ours(args):
             torch.cuda.synchronize()
         t_plain = p0.elapsed_time(p1)
         if args.plain_energies:
-            np.savez(args.plain_energies, ecorr=pe, status=pst, ms=t_plain)
+            np.savez(args.plain_energies, ecorr=pe, status=pst, ms=t_plain, key=key)
     if not args.no_subset:
         good = (pst == 0) & (status == 0)
         err = np.abs(ecorr - pe)[good]
