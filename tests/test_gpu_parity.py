@@ -72,6 +72,23 @@ def test_tran4_gen_rectangular_blocks(sys16):
     assert np.abs(out.cpu().numpy() - ref).max() < 1e-10
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("fp64tc5", 1e-10)])
+def test_tran4_gen_two_orbital_sets(sys16, precision, tol):
+    """The SAPT calls of tran4_gen (sapt_main.f90:435-522) put the orbitals of two monomers
+    in the four slots, e.g. 'TWOMOAB': A's occupied, A's active and virtual, B's occupied,
+    B's active and virtual. Here B's orbitals are an independent orthogonal rotation of
+    A's, so every slot holds different coefficients."""
+    s, G, *_ = sys16
+    CA = s.cmo
+    q, _ = np.linalg.qr(np.random.default_rng(21).standard_normal((s.n, s.n)))
+    CB = CA @ q
+    blocks = [CA[:, :s.nocc], CA[:, s.nin:], CB[:, :s.nocc], CB[:, s.nin:]]
+    ref = R.tran4_gen(s.n, *blocks, G)
+    out = api.tran4_gen(s.n, *[t(np.ascontiguousarray(b)) for b in blocks], t(G),
+                        precision=precision)
+    assert np.abs(out.cpu().numpy() - ref).max() < tol
+
+
 @pytest.mark.parametrize("lam", [0.0, 0.2113248654, 1.0])
 def test_ab_cas_fofo_matches_oracle(sys24, lam):
     s, G, ffoo, fofo = sys24
