@@ -208,10 +208,10 @@ int chol_eig(gc_context *ctx, int N, const double *abplus, const double *abmin, 
 int erpavec(gc_context *ctx, int N, double *abplus, double *abmin, double *Y, double *eig);
 
 // Integrand (gc_integrand.cu).
-// ERPA solutions of np points in the refined Cholesky form with sliced products, the
-// FP32 eigensolves of all points in one batched call: fill(k, ap, am) writes A+B and A-B
-// of point k into the two N x N buffers it is given, use(k, Y, eig) consumes that
-// point's Y (N x N) and omega (N).
+// ERPA solutions of np points in the refined Cholesky form with sliced products: the
+// Cholesky factors of all points in one batched launch chain and their FP32 eigensolves
+// in one batched call. fill(k, ap, am) writes A+B and A-B of point k into the two N x N
+// buffers it is given, use(k, Y, eig) consumes that point's Y (N x N) and omega (N).
 int erpa_solve_points(gc_context *ctx, int N, int np, int prec,
                       const std::function<int(int, double *, double *)> &fill,
                       const std::function<int(int, const double *, double *)> &use);
