@@ -310,8 +310,11 @@ def run_reference(args):
         cpu_port_energies([systems[0]], args.ngrid, log=lambda *a: None)
     per = [[] for _ in systems]
     sdims = [0] * len(systems)
+    nrev = min(4, len(systems))  # strata revisited after the first pass: the cheapest ones
     for k in range(args.steps):
-        j = k % len(systems)
+        # one pass over all strata, then the cheapest strata again, so that a long --steps
+        # run stays within minutes (the value uses each stratum's mean time)
+        j = k if k < len(systems) else (k - len(systems)) % nrev
         t, _, d = cpu_port_energies([systems[j]], args.ngrid, log=log)
         per[j] += t
         sdims[j] = d[0]
@@ -326,7 +329,8 @@ def run_reference(args):
               f"point with OpenMP, ERPASYMM1 with two LAPACK dsyevd, BLAS products), "
               f"{args.ngrid} points; the batch ordered by ERPA dimension in {len(systems)} strata "
               f"of {CPU_STRATUM}, one step = the median system of the next stratum (N "
-              f"{[sdims[j] for j in reached]}); value = strata reached / sum of their mean "
+              f"{[sdims[j] for j in reached]}; after one pass the {nrev} smallest strata are "
+              f"revisited); value = strata reached / sum of their mean "
               f"times" + ("" if len(reached) == len(systems) else
                           f" ({len(reached)} of {len(systems)} strata reached: biased to the "
                           f"smaller systems)"))
