@@ -74,17 +74,19 @@ int gc_synchronize(gc_context *ctx);
 /* Number of kernels of this library launched on the context so far. */
 long long gc_kernel_launches(const gc_context *ctx);
 /* Device time (CUDA events) of the cuSOLVER eigensolves run on the context so far
- * (dsyevd of ERPASYMM1 and of the Cholesky form, ssyevd of the refined form), and
- * their number; batched calls add their workers' eigensolves. No counterpart in
+ * (dsyevd of ERPASYMM1 and of the Cholesky form, ssyevd of the refined form, and in
+ * batched calls one cusolverDnXsyevBatched per system for all its points), and the
+ * number of matrices solved; batched calls add their workers' eigensolves. No counterpart in
  * the reference. */
 int gc_eig_time(const gc_context *ctx, double *ms, long long *calls);
 /* Phases of the AC path whose device time gc_phase_time reports. */
 enum gc_phase {
   GC_PHASE_TRANSFORM = 0, /* FOFO and FFOO (tran4_gen / tran4_factored) */
   GC_PHASE_ASSEMBLY = 1,  /* A+-B at a point (assembly or the affine combination) */
-  GC_PHASE_CHOLESKY = 2,  /* Cholesky factor of A+B */
+  GC_PHASE_CHOLESKY = 2,  /* Cholesky factor of A+B (in batched calls one per system) */
   GC_PHASE_PRODUCTS = 3,  /* the ERPA solve's products: L^T A- L, Y = L U (or A+^1/2) */
-  GC_PHASE_EIGEN = 4,     /* eigenpairs: dsyevd, or ssyevd plus the FP64 refinement */
+  GC_PHASE_EIGEN = 4,     /* eigenpairs: dsyevd, or the FP32 eigensolve plus the FP64
+                             refinement (in batched calls one phase per system) */
   GC_PHASE_INTEGRAND = 5, /* ACEneERPA */
   GC_PHASE_COUNT = 6
 };
