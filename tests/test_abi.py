@@ -66,3 +66,28 @@ def test_fortran_module_binds_declared_symbols():
     declared = set(declared_symbols())
     for nm in names:
         assert nm in declared or nm in {"cudaMalloc", "cudaFree", "cudaMemcpy"}, nm
+
+
+def test_header_is_c99_and_every_symbol_links(lib, tmp_path):
+    """The header is plain C (a C or Fortran host includes or binds it, not C++): a C99
+    program that takes the address of every declared entry point compiles with
+    -pedantic -Werror, links against the library and runs."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    syms = declared_symbols()
+    src = tmp_path / "abi.c"
+    src.write_text('#include "gammcor_gpu.h"\n#include <stdio.h>\n'
+                   "typedef void (*fn)(void);\nint main(void) {\n  fn p[] = {"
+                   + ", ".join(f"(fn){s}" for s in syms)
+                   + '};\n  printf("%d\\n", (int)(sizeof p / sizeof p[0]));\n  return 0;\n}\n')
+    exe = tmp_path / "abi"
+    libdir = ROOT / "gammcor_gb300"
+    cc = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                         "-I", str(ROOT / "include"), str(src), "-L", str(libdir),
+                         "-lgammcor_gpu", f"-Wl,-rpath,{libdir}", "-o", str(exe)],
+                        capture_output=True, text=True)
+    assert cc.returncode == 0, cc.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0 and int(run.stdout) == len(syms), run.stderr
