@@ -589,8 +589,10 @@ def run_ours(args):
         method = {"precision": args.precision,
                   "erpa": ("cholesky(A+B), affine A+-B, " +
                            ("FP32 eigensolve refined to FP64 accuracy "
-                            f"({args.eig_refine} iteration(s))"
+                            f"({args.eig_refine} iteration(s)); the Cholesky factors and FP32 "
+                            "eigensolves of a system's points batched"
                             if args.erpa == "refined" else "FP64 dsyevd")),
+                  "gemm_tile": args.tile or "chosen per product",
                   "streams": args.nstreams, "streams_autotune": tuned,
                   "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens else "off"),
                   "eig_emulation": bool(args.eig_emulation)}
