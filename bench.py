@@ -592,7 +592,7 @@ def run_ours(args):
                             f"({args.eig_refine} iteration(s)); the Cholesky factors and FP32 "
                             "eigensolves of a system's points batched"
                             if args.erpa == "refined" else "FP64 dsyevd")),
-                  "gemm_tile": args.tile or "chosen per product",
+                  "gemm_tile": "chosen per product (oz_tile)",
                   "streams": args.nstreams, "streams_autotune": tuned,
                   "surrogate": (f"ensemble gate at {args.threshold:g} Eh" if ens else "off"),
                   "eig_emulation": bool(args.eig_emulation)}
