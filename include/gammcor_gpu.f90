@@ -110,6 +110,35 @@ module gammcor_gpu
       type(gc_ac_params) :: par
       real(c_double) :: ecorr(*), ecas(*)
     end function
+    ! context settings and timing (no counterpart in the reference)
+    integer(c_int) function gc_set_eig_batch(ctx, on) bind(C, name="gc_set_eig_batch")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function gc_set_gemm_tile(ctx, width) bind(C, name="gc_set_gemm_tile")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: width
+    end function
+    integer(c_int) function gc_set_phase_timing(ctx, on) bind(C, name="gc_set_phase_timing")
+      import :: c_ptr, c_int
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: on
+    end function
+    integer(c_int) function gc_phase_time(ctx, phase, ms, calls) bind(C, name="gc_phase_time")
+      import :: c_ptr, c_int, c_double, c_long_long
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: phase
+      real(c_double) :: ms
+      integer(c_long_long) :: calls
+    end function
+    integer(c_int) function gc_eig_time(ctx, ms, calls) bind(C, name="gc_eig_time")
+      import :: c_ptr, c_int, c_double, c_long_long
+      type(c_ptr), value :: ctx
+      real(c_double) :: ms
+      integer(c_long_long) :: calls
+    end function
     ! CUDA runtime
     integer(c_int) function cudaMalloc(ptr, bytes) bind(C, name="cudaMalloc")
       import :: c_ptr, c_int, c_size_t
